@@ -1,0 +1,296 @@
+"""Benchmark of the MPCD step on GB300: particle-steps/s and the HBM roofline.
+
+Workload (default, one GPU): SRD Poiseuille channel, 1000 x 1000 x 20 fluid cells
+plus two wall layers in z, n = 20 particles per cell (N = 4.0e8), T = 1,
+g = 0.001, dt = 0.02, alpha = 120 deg, Philox seed 0; W warm-up steps, then K
+timed steps.  Synthetic data (random initial state), as in the reference's own
+benchmark (benchmark.py:36-47).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+One JSON line on rank 0.  `value` is device-timed particle-steps/s with the
+state resident in HBM; `e2e` is the same metric through the Python API the
+reference exposes (Simulation.step_and_sample + get_mean_fields, host wall
+clock, results read back to the host).  `--impl reference` times the
+reference's CPU step (the oracle's restatement of it; the reference binary
+where it was built) on the host cores on bounded slabs of the same workload.
+Several GPUs run independent replicas (the step has no exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MPCD particle-steps/sec on 1 GB300, % HBM peak; batched & adjoint vs plain"
+UNIT = "particle-steps/s"
+WORKLOAD = dict(L=(1000, 1000, 22), periodic=(1, 1, 0), n=20, dt=0.02, drag=0.001, temperature=1.0, seed=0)
+WORKLOAD_NAME = ("SRD Poiseuille channel 1000x1000x20 cells (+2 wall layers in z), n=20, N=4.0e8, T=1, "
+                 "g=0.001, dt=0.02, alpha=120deg, Philox seed 0")
+# Published reference number for this workload: 94 ms/step on an Ampere GPU
+# ("optimized" kernel, README.md:41) = 4.0e8 / 0.094 s.
+REFERENCE_PUBLISHED = 4.0e8 / 0.094
+ALGO_BYTES_PER_PARTICLE = 48.0   # read + write FP32 position and velocity once per step
+CPU_SLAB = dict(L=(1000, 2, 22), periodic=(1, 1, 0), n=20, dt=0.02, drag=0.001)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def ncu_traffic_per_particle():
+    """DRAM bytes per particle of the step kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "step_kernel_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["dram_bytes_per_particle"]), d.get("source", path)
+    except Exception:
+        return None, None
+
+
+# ---------------------------------------------------------------- CPU (oracle) timing
+
+def cpu_rate(threads: int, warmup: int, steps: int):
+    """Aggregate particle-steps/s of `threads` independent slabs advanced by the
+    restated reference step; returns (rate, particles per thread, kind)."""
+    import oracle as O
+
+    box = O.Box(L=CPU_SLAB["L"], periodic=CPU_SLAB["periodic"], n=CPU_SLAB["n"], dt=CPU_SLAB["dt"],
+                drag=CPU_SLAB["drag"])
+    runs = [O.Run(box, 1000 + t) for t in range(threads)]
+    barrier = threading.Barrier(threads + 1)
+    times = [0.0] * threads
+
+    def work(t):
+        runs[t].steps(warmup)
+        barrier.wait()
+        t0 = time.perf_counter()
+        runs[t].steps(steps)
+        times[t] = time.perf_counter() - t0
+        barrier.wait()
+
+    ths = [threading.Thread(target=work, args=(t,)) for t in range(threads)]
+    for th in ths:
+        th.start()
+    barrier.wait()
+    barrier.wait()
+    for th in ths:
+        th.join()
+    n = runs[0].N
+    for r in runs:
+        r.close()
+    return threads * n * steps / max(times), n
+
+
+def run_reference_arm(args, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    rate, n = cpu_rate(threads, args.warmup, args.steps)
+    sample = (f"{threads} independent slabs of the workload, each {CPU_SLAB['L'][0]}x{CPU_SLAB['L'][1]}x"
+              f"{CPU_SLAB['L'][2] - 2} cells + walls, n=20 ({n} particles), advanced by the restated reference "
+              f"CPU step; {args.warmup} warm-up + {args.steps} timed steps")
+    out = {"metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": threads * n / rate * 1e3,
+           "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": WORKLOAD_NAME, "sample": "per-thread slabs of the same workload"},
+           "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+
+def run_gpu_arm(args, rank, world, local_rank):
+    import torch
+
+    from cudampcd_gb300 import capi
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    wl = dict(WORKLOAD)
+    h = capi.Handle(L=wl["L"], periodic=wl["periodic"], n=wl["n"], dt=wl["dt"], drag=wl["drag"],
+                    temperature=wl["temperature"], seed=wl["seed"] + rank, device_id=local_rank)
+    N, C = h.N, h.C
+    h.step(args.warmup)
+    h.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks:
+        total_ms, kernel_ms = h.time_steps(args.steps)
+    torch.cuda.synchronize()
+    overflowed, flags = h.counters()
+    h.close()
+    elapsed = total_ms
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = world * N * args.steps / (elapsed * 1e-3)
+
+    # end to end through the Python API: step_and_sample + get_mean_fields
+    import cudampcd_gb300 as pympcd
+
+    params = pympcd.Params()
+    params.n = wl["n"]
+    params.temperature = wl["temperature"]
+    params.volume_size = (wl["L"][0], wl["L"][1], wl["L"][2] - 2)
+    params.periodicity = wl["periodic"]
+    params.drag = wl["drag"]
+    params.delta_t = wl["dt"]
+    params.algorithm = "srd"
+    params.device_id = local_rank
+    params.seed = wl["seed"] + rank
+    sim = pympcd.Simulation(params, "cuda")
+    sim.step_and_sample(min(args.warmup, 5))
+    sim.get_mean_fields()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    sim.step_and_sample(args.steps)
+    density, velocity = sim.get_mean_fields()
+    e2e_s = time.perf_counter() - t0
+    del sim
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * N * args.steps / e2e_s
+    d2h = (density.nbytes + velocity.nbytes) / args.steps
+
+    if rank == 0:
+        peak, peak_kind = peaks()
+        per_launch_ms = kernel_ms / args.steps
+        achieved = ALGO_BYTES_PER_PARTICLE * N / (per_launch_ms * 1e-3) / 1e9
+        bpp, src = ncu_traffic_per_particle()
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": value / (world * REFERENCE_PUBLISHED), "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD_NAME, "particles_per_gpu": N, "cells_per_gpu": C,
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2: 25.6 GB of particle state read and written per step",
+                       "vs_baseline_ref": "reference README.md:41, 94 ms/step on an Ampere GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": bpp * N if bpp else None, "traffic_source": src,
+                         "algorithmic_bytes_per_particle": ALGO_BYTES_PER_PARTICLE,
+                         "kernel": "step_kernel<SRD, Philox>", "kernel_ms": per_launch_ms},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,
+                    "api": "cudampcd_gb300.Simulation.step_and_sample + get_mean_fields (host wall clock)"},
+            "clocks": clocks.summary(),
+            "gpu_launches": args.steps,
+            "device_counters": {"bucket_overflows": overflowed, "error_flags": flags},
+        }
+        if not args.no_cpu:
+            threads = min(os.cpu_count() or 1, 16)
+            rate, n = cpu_rate(threads, 1, args.steps_cpu)
+            out["cpu_baseline"] = {
+                "value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": f"{threads} threads x one {CPU_SLAB['L']} slab ({n} particles), "
+                          f"{args.steps_cpu} steps of the restated reference CPU step"}
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=100)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--steps-cpu", dest="steps_cpu", type=int, default=8)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("at least 3 warm-up steps")
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", args.gpus))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        run_reference_arm(args, rank)
+    else:
+        run_gpu_arm(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

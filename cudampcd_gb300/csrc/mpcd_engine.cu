@@ -1,0 +1,816 @@
+// Host engine of the GB300 MPCD step and the C ABI of include/mpcd_gb.h.
+//
+// One handle = one simulation on one GPU: its device buffers, one CUDA stream,
+// the step counter that keys every Philox draw, and the sampling state machine
+// of the reference (cuda_backend_impl.cu:182-218).  No call synchronises
+// except the getters, the sample read-out and the error check at the end of
+// step()/step_and_sample().
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/mpcd_gb.h"
+#include "mpcd_kernels.h"
+
+namespace mpcd_gb {
+namespace {
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+// ---------------------------------------------------------------- host Philox (same draw model as the device)
+void philox_host(uint32_t c[4], uint32_t k0, uint32_t k1)
+{
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = (uint32_t)p1;
+        c[2] = n2;
+        c[3] = (uint32_t)p0;
+    }
+}
+
+void shift_host(const BoxDesc& b, uint64_t step, float out[3])
+{
+    uint32_t c[4] = {0u, (uint32_t)step, 1u | ((uint32_t)(step >> 32) << 8), 0u};
+    philox_host(c, b.seed_lo, b.seed_hi);
+    for (int i = 0; i < 3; ++i) out[i] = (float)(c[i] >> 8) * 0x1p-24f - 0.5f;
+}
+
+struct DeviceBuffer {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DeviceBuffer() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t alloc(size_t n)
+    {
+        release();
+        if (n == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        else p = nullptr;
+        return e;
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+class Error : public std::exception {
+public:
+    Error(int code, std::string msg) : code_(code), msg_(std::move(msg)) {}
+    const char* what() const noexcept override { return msg_.c_str(); }
+    int code() const { return code_; }
+
+private:
+    int code_;
+    std::string msg_;
+};
+
+void check(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw Error(e == cudaErrorMemoryAllocation ? MPCD_GB_ENOMEM : MPCD_GB_ECUDA,
+                    std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+}  // namespace
+
+class Engine {
+public:
+    explicit Engine(const mpcd_gb_params& p) : params_(p)
+    {
+        validate();
+        check(cudaSetDevice((int)p.device_id), "cudaSetDevice");
+        check(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+        stream_ = own_stream_;
+        cudaDeviceProp prop;
+        check(cudaGetDeviceProperties(&prop, (int)p.device_id), "cudaGetDeviceProperties");
+        sms_ = prop.multiProcessorCount;
+        build_boxes();
+        allocate();
+        configure();
+        initialise();
+    }
+
+    ~Engine()
+    {
+        if (own_stream_) {
+            cudaStreamSynchronize(own_stream_);
+            cudaStreamDestroy(own_stream_);
+        }
+    }
+
+    // ------------------------------------------------------------ reference Backend interface
+    void step(int n, bool sample)
+    {
+        if (n < 0) throw Error(MPCD_GB_EINVAL, "negative step count");
+        for (int i = 0; i < n; ++i) {
+            const bool snapshot = sample && !sampling_;
+            launch_one_step(sample);
+            if (sample) {
+                check(launch_sample_finalize(samp_.as<float4>(), acc_.as<SampleAcc>(), cells_, snapshot ? 1 : 0,
+                                             sms_ * 8, stream_),
+                      "sample finalize");
+                if (snapshot) {
+                    sampling_ = true;
+                    sample_counter_ = 0;
+                } else {
+                    ++sample_counter_;
+                }
+            }
+        }
+        check_device_errors();
+    }
+
+    void sample_mean(float* density, float* velocity)
+    {
+        std::vector<SampleAcc> acc(cells_);
+        check(cudaMemcpyAsync(acc.data(), acc_.p, sizeof(SampleAcc) * cells_, cudaMemcpyDeviceToHost, stream_),
+              "sample read");
+        check(cudaStreamSynchronize(stream_), "sample read");
+        // cpu_backend.cpp:218 / cuda_backend_impl.cu:210: divide by the counter, S-1 for S samples
+        const double inverse = 1.0 / (double)sample_counter_;
+        const BoxDesc& b = boxes_[0];
+        for (uint32_t c = 0; c < b.C; ++c) {
+            density[c] = (float)(acc[c].n * inverse);
+            velocity[3 * c + 0] = (float)(acc[c].vx * inverse);
+            velocity[3 * c + 1] = (float)(acc[c].vy * inverse);
+            velocity[3 * c + 2] = (float)(acc[c].vz * inverse);
+        }
+        sampling_ = false;
+    }
+
+    void get(float* pos, float* vel)
+    {
+        gather(dense_pos_.as<float>(), dense_vel_.as<float>());
+        if (pos)
+            check(cudaMemcpyAsync(pos, dense_pos_.p, sizeof(float) * 3 * N_, cudaMemcpyDeviceToHost, stream_),
+                  "positions read");
+        if (vel)
+            check(cudaMemcpyAsync(vel, dense_vel_.p, sizeof(float) * 3 * N_, cudaMemcpyDeviceToHost, stream_),
+                  "velocities read");
+        check(cudaStreamSynchronize(stream_), "particle read");
+    }
+
+    void set(const float* pos, const float* vel)
+    {
+        if (!pos || !vel) gather(dense_pos_.as<float>(), dense_vel_.as<float>());
+        if (pos)
+            check(cudaMemcpyAsync(dense_pos_.p, pos, sizeof(float) * 3 * N_, cudaMemcpyHostToDevice, stream_),
+                  "positions write");
+        if (vel)
+            check(cudaMemcpyAsync(dense_vel_.p, vel, sizeof(float) * 3 * N_, cudaMemcpyHostToDevice, stream_),
+                  "velocities write");
+        scatter_dense();
+        check(cudaStreamSynchronize(stream_), "particle write");
+        check_device_errors();
+    }
+
+    void dump(uint32_t* cell, uint32_t* slot, uint32_t* prev, uint32_t* id, uint32_t* counts)
+    {
+        DeviceBuffer dc, ds, dp, di;
+        check(dc.alloc(sizeof(uint32_t) * N_), "dump alloc");
+        check(ds.alloc(sizeof(uint32_t) * N_), "dump alloc");
+        check(dp.alloc(sizeof(uint32_t) * N_), "dump alloc");
+        check(di.alloc(sizeof(uint32_t) * N_), "dump alloc");
+        layout(dc.as<uint32_t>(), ds.as<uint32_t>(), dp.as<uint32_t>(), di.as<uint32_t>());
+        if (cell) check(cudaMemcpyAsync(cell, dc.p, sizeof(uint32_t) * N_, cudaMemcpyDeviceToHost, stream_), "dump");
+        if (slot) check(cudaMemcpyAsync(slot, ds.p, sizeof(uint32_t) * N_, cudaMemcpyDeviceToHost, stream_), "dump");
+        if (prev) check(cudaMemcpyAsync(prev, dp.p, sizeof(uint32_t) * N_, cudaMemcpyDeviceToHost, stream_), "dump");
+        if (id) check(cudaMemcpyAsync(id, di.p, sizeof(uint32_t) * N_, cudaMemcpyDeviceToHost, stream_), "dump");
+        check(cudaStreamSynchronize(stream_), "dump");
+        sort_overflow_tail(cell, slot, prev, id);
+        if (counts) {
+            std::vector<uint32_t> raw(cells_);
+            check(cudaMemcpyAsync(raw.data(), count_[parity()].p, sizeof(uint32_t) * cells_, cudaMemcpyDeviceToHost,
+                                  stream_),
+                  "dump");
+            check(cudaStreamSynchronize(stream_), "dump");
+            const BoxDesc& b = boxes_[0];
+            for (uint32_t s = 0; s < b.C; ++s) {
+                const uint32_t Lz = (uint32_t)b.L[2], Lx = (uint32_t)b.L[0];
+                const uint32_t z = s % Lz, col = s / Lz, x = col % Lx, y = col / Lx;
+                counts[x + Lx * (y + (uint32_t)b.L[1] * z)] = raw[s];
+            }
+        }
+        check(cudaStreamSynchronize(stream_), "dump");
+    }
+
+    // The overflow list is filled in arrival order; order its part of a dump by
+    // (cell, prev) so that a dump is deterministic.
+    void sort_overflow_tail(uint32_t* cell, uint32_t* slot, uint32_t* prev, uint32_t* id)
+    {
+        DeviceState st;
+        check(cudaMemcpy(&st, state_.p, sizeof st, cudaMemcpyDeviceToHost), "dump");
+        const uint64_t m = std::min(st.ov_count[parity()], ov_cap_);
+        if (m < 2 || !cell || !prev) return;
+        const uint64_t base = N_ - m;
+        std::vector<uint64_t> order(m);
+        for (uint64_t i = 0; i < m; ++i) order[i] = i;
+        std::sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) {
+            const uint32_t ca = cell[base + a], cb = cell[base + b];
+            return ca != cb ? ca < cb : prev[base + a] < prev[base + b];
+        });
+        auto permute = [&](uint32_t* v) {
+            if (!v) return;
+            std::vector<uint32_t> t(m);
+            for (uint64_t i = 0; i < m; ++i) t[i] = v[base + order[i]];
+            std::copy(t.begin(), t.end(), v + base);
+        };
+        permute(cell);
+        permute(slot);
+        permute(prev);
+        permute(id);
+    }
+
+    // ------------------------------------------------------------ hooks
+    void inject_shift(uint64_t step, const float s[3])
+    {
+        int slot = -1;
+        for (int i = 0; i < kMaxInjectedShifts; ++i)
+            if (inject_valid_[i] && inject_step_[i] == step) slot = i;
+        for (int i = 0; i < kMaxInjectedShifts && slot < 0; ++i)
+            if (!inject_valid_[i] || inject_step_[i] < step_) slot = i;
+        if (slot < 0) throw Error(MPCD_GB_ESTATE, "too many pending injected shifts");
+        inject_valid_[slot] = 1;
+        inject_step_[slot] = step;
+        for (int d = 0; d < 3; ++d) inject_shift_[slot][d] = s[d];
+        sync_injections();
+    }
+
+    void get_shift(uint64_t step, float out[3]) const
+    {
+        for (int i = 0; i < kMaxInjectedShifts; ++i)
+            if (inject_valid_[i] && inject_step_[i] == step) {
+                for (int d = 0; d < 3; ++d) out[d] = inject_shift_[i][d];
+                return;
+            }
+        shift_host(boxes_[0], step, out);
+    }
+
+    void inject_draws(uint32_t gmax, uint32_t pmax, const uint32_t* ghost_count, const float* ghost_pos,
+                      const float* ghost_vel, const float* axis, const float* gate_u, const float* gauss)
+    {
+        if (!ghost_count || !axis) {
+            use_table_ = false;
+            return;
+        }
+        const size_t C = boxes_[0].C;
+        check(t_count_.alloc(sizeof(uint32_t) * C), "draws alloc");
+        check(t_gpos_.alloc(sizeof(float) * C * gmax * 3 + 16), "draws alloc");
+        check(t_gvel_.alloc(sizeof(float) * C * gmax * 3 + 16), "draws alloc");
+        check(t_axis_.alloc(sizeof(float) * C * 3), "draws alloc");
+        check(t_gate_.alloc(sizeof(float) * C), "draws alloc");
+        check(t_gauss_.alloc(sizeof(float) * C * pmax + 16), "draws alloc");
+        auto up = [&](DeviceBuffer& d, const void* h, size_t n) {
+            if (h && n) check(cudaMemcpyAsync(d.p, h, n, cudaMemcpyHostToDevice, stream_), "draws upload");
+            else check(cudaMemsetAsync(d.p, 0, d.bytes, stream_), "draws upload");
+        };
+        up(t_count_, ghost_count, sizeof(uint32_t) * C);
+        up(t_gpos_, ghost_pos, sizeof(float) * C * gmax * 3);
+        up(t_gvel_, ghost_vel, sizeof(float) * C * gmax * 3);
+        up(t_axis_, axis, sizeof(float) * C * 3);
+        up(t_gate_, gate_u, sizeof(float) * C);
+        up(t_gauss_, gauss, sizeof(float) * C * pmax);
+        tables_ = DrawTables{t_count_.as<uint32_t>(), t_gpos_.as<float>(), t_gvel_.as<float>(), t_axis_.as<float>(),
+                             t_gate_.as<float>(), t_gauss_.as<float>(), gmax, pmax};
+        check(cudaStreamSynchronize(stream_), "draws upload");
+        use_table_ = true;
+    }
+
+    void counters(uint64_t out[2])
+    {
+        DeviceState st;
+        check(cudaMemcpyAsync(&st, state_.p, sizeof st, cudaMemcpyDeviceToHost, stream_), "counters");
+        check(cudaStreamSynchronize(stream_), "counters");
+        out[0] = st.overflow_total;
+        out[1] = st.error_flags;
+    }
+
+    void set_stream(void* s) { stream_ = s ? static_cast<cudaStream_t>(s) : own_stream_; }
+    void synchronize() { check(cudaStreamSynchronize(stream_), "synchronize"); }
+
+    void time_steps(int n, float* total_ms, float* kernel_ms)
+    {
+        cudaEvent_t e0, e1;
+        check(cudaEventCreate(&e0), "event");
+        check(cudaEventCreate(&e1), "event");
+        std::vector<cudaEvent_t> ks(2 * (size_t)n);
+        for (auto& e : ks) check(cudaEventCreate(&e), "event");
+        check(cudaEventRecord(e0, stream_), "event");
+        for (int i = 0; i < n; ++i) {
+            check(cudaEventRecord(ks[2 * i], stream_), "event");
+            launch_one_step(false);
+            check(cudaEventRecord(ks[2 * i + 1], stream_), "event");
+        }
+        check(cudaEventRecord(e1, stream_), "event");
+        check(cudaEventSynchronize(e1), "event");
+        float t = 0, k = 0;
+        check(cudaEventElapsedTime(&t, e0, e1), "event");
+        for (int i = 0; i < n; ++i) {
+            float dt = 0;
+            check(cudaEventElapsedTime(&dt, ks[2 * i], ks[2 * i + 1]), "event");
+            k += dt;
+        }
+        for (auto& e : ks) cudaEventDestroy(e);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (total_ms) *total_ms = t;
+        if (kernel_ms) *kernel_ms = k;
+        check_device_errors();
+    }
+
+    size_t num_particles() const { return N_; }
+    size_t num_cells() const { return boxes_[0].C; }
+    uint64_t step_index() const { return step_; }
+
+private:
+    unsigned parity() const { return (unsigned)(step_ & 1); }
+
+    void validate()
+    {
+        const mpcd_gb_params& p = params_;
+        for (int d = 0; d < 3; ++d) {
+            const float L = p.volume_size[d];
+            if (!(L >= 1.0f) || L != std::floor(L) || L > 65536.0f)
+                throw Error(MPCD_GB_EINVAL, "volume_size must hold positive integers");
+            if (p.periodicity[d] != 0 && p.periodicity[d] != 1)
+                throw Error(MPCD_GB_EINVAL, "periodicity must be 0 or 1");
+            if (!p.periodicity[d] && L < 3.0f) throw Error(MPCD_GB_EINVAL, "a walled axis needs at least 3 layers");
+        }
+        if (p.n < 1) throw Error(MPCD_GB_EINVAL, "n must be at least 1");
+        if (p.algorithm != 0 && p.algorithm != 1) throw Error(MPCD_GB_EINVAL, "algorithm must be srd or extended");
+        if (p.experiment != 0 && p.experiment != 1) throw Error(MPCD_GB_EINVAL, "experiment must be standard or channel");
+        if (!(p.delta_t > 0.0f) || !std::isfinite(p.delta_t)) throw Error(MPCD_GB_EINVAL, "delta_t must be positive");
+        if (!std::isfinite(p.thermal_velocity) || p.thermal_velocity < 0.0f)
+            throw Error(MPCD_GB_EINVAL, "thermal_velocity must be finite and non-negative");
+        if (!std::isfinite(p.drag)) throw Error(MPCD_GB_EINVAL, "drag must be finite");
+    }
+
+    void build_boxes()
+    {
+        const mpcd_gb_params& p = params_;
+        BoxDesc b{};
+        uint64_t Nf = p.n;
+        for (int d = 0; d < 3; ++d) {
+            b.L[d] = (int32_t)p.volume_size[d];
+            b.Lf[d] = p.volume_size[d];
+            b.periodic[d] = p.periodicity[d];
+            Nf *= (uint64_t)(b.L[d] - 2 * (1 - b.periodic[d]));
+        }
+        b.wall_z = !p.periodicity[2];
+        b.channel = p.experiment == 1;
+        b.dt = p.delta_t;
+        b.drag_dt = p.drag * p.delta_t;
+        b.tv = p.thermal_velocity;
+        b.R2 = (b.Lf[2] - 2) * (b.Lf[2] - 2) * 0.25f;
+        // simulation_functions.cpp:118-119: sinf / cosf of 120 degrees in float
+        b.sin_a = sinf((float)((M_PI * 120) / 180));
+        b.cos_a = cosf((float)((M_PI * 120) / 180));
+        b.n = p.n;
+        b.cap = 4 * p.n;
+        const uint64_t C = (uint64_t)b.L[0] * b.L[1] * b.L[2];
+        if (C >= (1ull << 31)) throw Error(MPCD_GB_EINVAL, "too many cells");
+        if (Nf >= (1ull << 32) - 1) throw Error(MPCD_GB_EINVAL, "too many particles");
+        b.C = (uint32_t)C;
+        b.N = (uint32_t)Nf;
+        b.cell_base = 0;
+        b.slot_base = 0;
+        b.dense_base = 0;
+        b.seed_lo = (uint32_t)p.seed;
+        b.seed_hi = (uint32_t)(p.seed >> 32);
+        pbuf_ = 1536;
+        if (5 * b.n > pbuf_) pbuf_ = 5 * b.n;
+        if (pbuf_ > 5000) throw Error(MPCD_GB_EINVAL, "n too large for one cell in shared memory");
+        uint32_t tc = (uint32_t)(pbuf_ / (1.2 * b.n));
+        tc = tc < 1 ? 1 : (tc > (uint32_t)kMaxTileCells ? (uint32_t)kMaxTileCells : tc);
+        b.tile_cells = tc;
+        b.tile_base = 0;
+        b.tiles = (b.C + tc - 1) / tc;
+        boxes_.assign(1, b);
+        N_ = Nf;
+        cells_ = C;
+        tiles_ = b.tiles;
+        total_slots_ = C * b.cap;
+        ov_cap_ = (uint32_t)std::max<uint64_t>(1u << 16, std::min<uint64_t>(N_, 1u << 22));
+        if (total_slots_ + ov_cap_ >= (1ull << 32))
+            throw Error(MPCD_GB_EINVAL, "cells * 4n exceeds the 32-bit slot space of one handle");
+        float table[13][3];
+        const int steps = 4;
+        for (int select = 0; select <= 12; ++select) {   // simulation_functions.cpp:272-290
+            const int phi_i = select % steps + 1, theta_i = select / steps + 1;
+            float theta, phi;
+            if ((theta_i % 2) && (phi_i % 2))
+                theta = theta_i == 1 ? 0.95531661812450927816f : (float)M_PI - 0.95531661812450927816f;
+            else
+                theta = theta_i * ((float)M_PI / steps);
+            phi = phi_i * ((float)M_PI / steps);
+            table[select][0] = sinf(theta) * cosf(phi);
+            table[select][1] = sinf(theta) * sinf(phi);
+            table[select][2] = cosf(theta);
+        }
+        std::memcpy(ext_axis_, table, sizeof table);
+    }
+
+    void allocate()
+    {
+        check(boxes_d_.alloc(sizeof(BoxDesc) * boxes_.size()), "alloc boxes");
+        check(cudaMemcpy(boxes_d_.p, boxes_.data(), sizeof(BoxDesc) * boxes_.size(), cudaMemcpyHostToDevice),
+              "upload boxes");
+        for (int k = 0; k < 2; ++k) {
+            check(pos_[k].alloc(sizeof(float4) * total_slots_), "alloc bucket positions");
+            check(vel_[k].alloc(sizeof(float4) * total_slots_), "alloc bucket velocities");
+            check(count_[k].alloc(sizeof(uint32_t) * cells_), "alloc counts");
+            check(cudaMemset(count_[k].p, 0, count_[k].bytes), "clear counts");
+            check(ov_pos_[k].alloc(sizeof(float4) * ov_cap_), "alloc overflow list");
+            check(ov_vel_[k].alloc(sizeof(float4) * ov_cap_), "alloc overflow list");
+        }
+        check(state_.alloc(sizeof(DeviceState)), "alloc state");
+        check(cudaMemset(state_.p, 0, sizeof(DeviceState)), "clear state");
+        check(samp_.alloc(sizeof(float4) * cells_), "alloc sample");
+        check(cudaMemset(samp_.p, 0, samp_.bytes), "clear sample");
+        check(acc_.alloc(sizeof(SampleAcc) * cells_), "alloc sample sums");
+        check(cudaMemset(acc_.p, 0, acc_.bytes), "clear sample sums");
+        check(dense_pos_.alloc(sizeof(float) * 3 * N_ + 16), "alloc dense positions");
+        check(dense_vel_.alloc(sizeof(float) * 3 * N_ + 16), "alloc dense velocities");
+        check(offsets_.alloc(sizeof(uint32_t) * (cells_ + 1)), "alloc offsets");
+        check(scan_status_.alloc(sizeof(unsigned long long) * scan_status_words(cells_)), "alloc scan status");
+        check(scan_counter_.alloc(sizeof(unsigned int)), "alloc scan counter");
+        check(partial_.alloc(sizeof(double) * 3 * kReduceBlocks), "alloc partial sums");
+    }
+
+    void configure()
+    {
+        int per_sm = 0;
+        check(configure_step(params_.algorithm, pbuf_, &per_sm), "configure step kernel");
+        if (per_sm < 1) throw Error(MPCD_GB_ECUDA, "step kernel does not fit on an SM");
+        grid_ = (int)std::min<uint64_t>(tiles_, (uint64_t)sms_ * per_sm);
+    }
+
+    void initialise()
+    {
+        check(launch_init(boxes_d_.as<BoxDesc>(), (int)boxes_.size(), dense_pos_.as<float>(), dense_vel_.as<float>(),
+                          N_, sms_ * 16, stream_),
+              "init");
+        // zero net momentum (BASELINE config 1 asks for it; the reference does not remove it)
+        check(launch_momentum_partial(dense_vel_.as<float>(), 0, N_, partial_.as<double>(), kReduceBlocks, stream_),
+              "momentum");
+        std::vector<double> part(3 * kReduceBlocks);
+        check(cudaMemcpyAsync(part.data(), partial_.p, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, stream_),
+              "momentum");
+        check(cudaStreamSynchronize(stream_), "momentum");
+        double m[3] = {0, 0, 0};
+        for (int i = 0; i < kReduceBlocks; ++i)
+            for (int d = 0; d < 3; ++d) m[d] += part[3 * i + d];
+        if (N_)
+            check(launch_subtract(dense_vel_.as<float>(), 0, N_, (float)(m[0] / N_), (float)(m[1] / N_),
+                                  (float)(m[2] / N_), sms_ * 16, stream_),
+                  "momentum");
+        scatter_dense();
+        check(cudaStreamSynchronize(stream_), "initialise");
+        check_device_errors();
+    }
+
+    StepArgs args() const
+    {
+        StepArgs a{};
+        a.boxes = boxes_d_.as<BoxDesc>();
+        a.nboxes = (int)boxes_.size();
+        a.num_tiles = (uint32_t)tiles_;
+        a.total_slots = total_slots_;
+        a.step = step_;
+        const unsigned p = parity(), q = p ^ 1u;
+        a.in_pos = pos_[p].as<float4>();
+        a.in_vel = vel_[p].as<float4>();
+        a.in_count = count_[p].as<uint32_t>();
+        a.out_pos = pos_[q].as<float4>();
+        a.out_vel = vel_[q].as<float4>();
+        a.out_count = count_[q].as<uint32_t>();
+        a.ov_in_pos = ov_pos_[p].as<float4>();
+        a.ov_in_vel = ov_vel_[p].as<float4>();
+        a.ov_out_pos = ov_pos_[q].as<float4>();
+        a.ov_out_vel = ov_vel_[q].as<float4>();
+        a.ov_cap = ov_cap_;
+        a.state = state_.as<DeviceState>();
+        a.samp = samp_.as<float4>();
+        std::memcpy(a.ext_axis, ext_axis_, sizeof ext_axis_);
+        a.draws = tables_;
+        return a;
+    }
+
+    void launch_one_step(bool sample)
+    {
+        StepArgs a = args();
+        a.sample = sample ? 1 : 0;
+        check(launch_step(a, params_.algorithm, use_table_, pbuf_, grid_, stream_), "step kernel");
+        use_table_ = false;
+        ++step_;
+    }
+
+    // Dense clean arrays -> buckets of the current parity (state before step step_).
+    void scatter_dense()
+    {
+        const unsigned p = parity();
+        check(cudaMemsetAsync(count_[p].p, 0, count_[p].bytes, stream_), "clear counts");
+        check(cudaMemsetAsync((char*)state_.p + offsetof(DeviceState, ov_count) + sizeof(unsigned int) * p, 0,
+                              sizeof(unsigned int), stream_),
+              "clear overflow list");
+        StepArgs a = args();
+        a.step = step_ - 1;   // the scatter plays the epilogue of the previous step
+        a.out_pos = pos_[p].as<float4>();
+        a.out_vel = vel_[p].as<float4>();
+        a.out_count = count_[p].as<uint32_t>();
+        a.ov_out_pos = ov_pos_[p].as<float4>();
+        a.ov_out_vel = ov_vel_[p].as<float4>();
+        check(launch_scatter(a, dense_pos_.as<float>(), dense_vel_.as<float>(), N_, sms_ * 8, stream_),
+              "scatter");
+    }
+
+    void gather(float* pos, float* vel)
+    {
+        const unsigned p = parity();
+        StepArgs a = args();
+        check(cudaMemsetAsync(scan_counter_.p, 0, sizeof(unsigned int), stream_), "gather");
+        check(launch_gather(a, count_[p].as<uint32_t>(), pos_[p].as<float4>(), vel_[p].as<float4>(), cells_, N_,
+                            ov_pos_[p].as<float4>(), ov_vel_[p].as<float4>(), p, pos, vel,
+                            scan_counter_.as<unsigned int>(), sms_ * 8, stream_),
+              "gather");
+        unsigned int seen = 0;
+        check(cudaMemcpyAsync(&seen, scan_counter_.p, sizeof seen, cudaMemcpyDeviceToHost, stream_), "gather");
+        check(cudaStreamSynchronize(stream_), "gather");
+        expect_count(seen);
+    }
+
+    void layout(uint32_t* cell, uint32_t* slot, uint32_t* prev, uint32_t* id)
+    {
+        const unsigned p = parity();
+        StepArgs a = args();
+        check(launch_layout(a, count_[p].as<uint32_t>(), pos_[p].as<float4>(), vel_[p].as<float4>(),
+                            offsets_.as<uint32_t>(), cells_, N_, scan_status_.as<unsigned long long>(),
+                            scan_counter_.as<unsigned int>(), ov_pos_[p].as<float4>(), ov_vel_[p].as<float4>(), p,
+                            cell, slot, prev, id, sms_ * 8, stream_),
+              "layout");
+        uint32_t total = 0;
+        check(cudaMemcpyAsync(&total, offsets_.as<uint32_t>() + cells_, sizeof total, cudaMemcpyDeviceToHost, stream_),
+              "layout");
+        DeviceState st;
+        check(cudaMemcpyAsync(&st, state_.p, sizeof st, cudaMemcpyDeviceToHost, stream_), "layout");
+        check(cudaStreamSynchronize(stream_), "layout");
+        expect_count((uint64_t)total + std::min(st.ov_count[p], ov_cap_));
+    }
+
+    void expect_count(uint64_t have)
+    {
+        if (have != N_) {
+            char msg[160];
+            std::snprintf(msg, sizeof msg, "particle count mismatch: %llu stored, %llu expected",
+                          (unsigned long long)have, (unsigned long long)N_);
+            throw Error(MPCD_GB_EDEVICE, msg);
+        }
+    }
+
+    void sync_injections()
+    {
+        DeviceState st;
+        check(cudaMemcpyAsync(&st, state_.p, sizeof st, cudaMemcpyDeviceToHost, stream_), "inject");
+        check(cudaStreamSynchronize(stream_), "inject");
+        for (int i = 0; i < kMaxInjectedShifts; ++i) {
+            st.inject_valid[i] = inject_valid_[i];
+            st.inject_step[i] = inject_step_[i];
+            for (int d = 0; d < 3; ++d) st.inject_shift[i][d] = inject_shift_[i][d];
+        }
+        check(cudaMemcpyAsync(state_.p, &st, sizeof st, cudaMemcpyHostToDevice, stream_), "inject");
+        check(cudaStreamSynchronize(stream_), "inject");
+    }
+
+    void check_device_errors()
+    {
+        check(cudaGetLastError(), "launch");
+        unsigned int flags = 0;
+        check(cudaMemcpyAsync(&flags, (char*)state_.p + offsetof(DeviceState, error_flags), sizeof flags,
+                              cudaMemcpyDeviceToHost, stream_),
+              "error flags");
+        check(cudaStreamSynchronize(stream_), "step");
+        if (flags & kErrOverflowListFull) throw Error(MPCD_GB_EDEVICE, "cell overflow list exhausted");
+        if (flags & kErrWaitTimeout) throw Error(MPCD_GB_EDEVICE, "device wait timed out");
+        if (flags & kErrKeyMismatch) throw Error(MPCD_GB_EDEVICE, "particle found in the wrong cell bucket");
+    }
+
+    static constexpr int kReduceBlocks = 1024;
+
+    mpcd_gb_params params_;
+    cudaStream_t own_stream_ = nullptr, stream_ = nullptr;
+    int sms_ = 0, grid_ = 0;
+    std::vector<BoxDesc> boxes_;
+    uint64_t N_ = 0, cells_ = 0, tiles_ = 0, total_slots_ = 0;
+    uint32_t ov_cap_ = 0, pbuf_ = 0;
+    float ext_axis_[13][3];
+    uint64_t step_ = 0;
+    bool sampling_ = false;
+    uint64_t sample_counter_ = 0;
+    bool use_table_ = false;
+    DrawTables tables_{};
+    int inject_valid_[kMaxInjectedShifts] = {0, 0, 0, 0};
+    uint64_t inject_step_[kMaxInjectedShifts] = {0, 0, 0, 0};
+    float inject_shift_[kMaxInjectedShifts][3] = {};
+    DeviceBuffer boxes_d_, pos_[2], vel_[2], count_[2], ov_pos_[2], ov_vel_[2], state_, samp_, acc_, dense_pos_,
+        dense_vel_, offsets_, scan_status_, scan_counter_, partial_;
+    DeviceBuffer t_count_, t_gpos_, t_gvel_, t_axis_, t_gate_, t_gauss_;
+};
+
+}  // namespace mpcd_gb
+
+// ==================================================================== C ABI
+
+struct mpcd_gb_handle {
+    mpcd_gb::Engine* engine = nullptr;
+    std::string error;
+};
+
+namespace {
+thread_local std::string g_create_error;
+
+template <class F>
+int32_t guarded(mpcd_gb_handle* h, F&& f)
+{
+    if (!h || !h->engine) return MPCD_GB_EINVAL;
+    try {
+        h->error.clear();
+        f(*h->engine);
+        return MPCD_GB_OK;
+    } catch (const mpcd_gb::Error& e) {
+        h->error = e.what();
+        return e.code();
+    } catch (const std::bad_alloc&) {
+        h->error = "host allocation failed";
+        return MPCD_GB_ENOMEM;
+    } catch (const std::exception& e) {
+        h->error = e.what();
+        return MPCD_GB_EINVAL;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int32_t mpcd_gb_abi_version(void) { return MPCD_GB_ABI_VERSION; }
+
+int32_t mpcd_gb_create(const mpcd_gb_params* params, mpcd_gb_handle** out)
+{
+    g_create_error.clear();
+    if (!params || !out) {
+        g_create_error = "null argument";
+        return MPCD_GB_EINVAL;
+    }
+    *out = nullptr;
+    auto* h = new (std::nothrow) mpcd_gb_handle;
+    if (!h) return MPCD_GB_ENOMEM;
+    try {
+        h->engine = new mpcd_gb::Engine(*params);
+    } catch (const mpcd_gb::Error& e) {
+        g_create_error = e.what();
+        delete h;
+        return e.code();
+    } catch (const std::exception& e) {
+        g_create_error = e.what();
+        delete h;
+        return MPCD_GB_ENOMEM;
+    }
+    *out = h;
+    return MPCD_GB_OK;
+}
+
+void mpcd_gb_destroy(mpcd_gb_handle* h)
+{
+    if (!h) return;
+    delete h->engine;
+    delete h;
+}
+
+const char* mpcd_gb_last_error(const mpcd_gb_handle* h)
+{
+    return h ? h->error.c_str() : g_create_error.c_str();
+}
+
+int32_t mpcd_gb_step(mpcd_gb_handle* h, int32_t n)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.step(n, false); });
+}
+
+int32_t mpcd_gb_step_and_sample(mpcd_gb_handle* h, int32_t n)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.step(n, true); });
+}
+
+int32_t mpcd_gb_get_sample_mean(mpcd_gb_handle* h, float* density, float* velocity)
+{
+    if (!density || !velocity) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.sample_mean(density, velocity); });
+}
+
+size_t mpcd_gb_num_particles(const mpcd_gb_handle* h) { return h && h->engine ? h->engine->num_particles() : 0; }
+
+size_t mpcd_gb_num_cells(const mpcd_gb_handle* h) { return h && h->engine ? h->engine->num_cells() : 0; }
+
+int32_t mpcd_gb_get_positions(mpcd_gb_handle* h, float* out)
+{
+    if (!out) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.get(out, nullptr); });
+}
+
+int32_t mpcd_gb_get_velocities(mpcd_gb_handle* h, float* out)
+{
+    if (!out) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.get(nullptr, out); });
+}
+
+int32_t mpcd_gb_set_positions(mpcd_gb_handle* h, const float* in)
+{
+    if (!in) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.set(in, nullptr); });
+}
+
+int32_t mpcd_gb_set_velocities(mpcd_gb_handle* h, const float* in)
+{
+    if (!in) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.set(nullptr, in); });
+}
+
+int32_t mpcd_gb_set_particles(mpcd_gb_handle* h, const float* positions, const float* velocities)
+{
+    if (!positions || !velocities) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.set(positions, velocities); });
+}
+
+int32_t mpcd_gb_set_stream(mpcd_gb_handle* h, void* stream)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.set_stream(stream); });
+}
+
+int32_t mpcd_gb_synchronize(mpcd_gb_handle* h)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.synchronize(); });
+}
+
+int32_t mpcd_gb_time_steps(mpcd_gb_handle* h, int32_t n_steps, float* total_ms, float* kernel_ms)
+{
+    if (n_steps < 0) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.time_steps(n_steps, total_ms, kernel_ms); });
+}
+
+uint64_t mpcd_gb_step_index(const mpcd_gb_handle* h) { return h && h->engine ? h->engine->step_index() : 0; }
+
+int32_t mpcd_gb_inject_shift(mpcd_gb_handle* h, uint64_t step, const float shift[3])
+{
+    if (!shift) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.inject_shift(step, shift); });
+}
+
+int32_t mpcd_gb_get_shift(mpcd_gb_handle* h, uint64_t step, float shift[3])
+{
+    if (!shift) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.get_shift(step, shift); });
+}
+
+int32_t mpcd_gb_dump_layout(mpcd_gb_handle* h, uint32_t* cell, uint32_t* slot, uint32_t* prev, uint32_t* id,
+                            uint32_t* counts)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.dump(cell, slot, prev, id, counts); });
+}
+
+int32_t mpcd_gb_inject_draws(mpcd_gb_handle* h, uint32_t gmax, uint32_t pmax, const uint32_t* ghost_count,
+                             const float* ghost_pos, const float* ghost_vel, const float* axis, const float* gate_u,
+                             const float* gauss)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) {
+        e.inject_draws(gmax, pmax, ghost_count, ghost_pos, ghost_vel, axis, gate_u, gauss);
+    });
+}
+
+int32_t mpcd_gb_counters(mpcd_gb_handle* h, uint64_t out[2])
+{
+    if (!out) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.counters(out); });
+}
+
+}  // extern "C"

@@ -1,0 +1,1130 @@
+// Kernels of the GB300 MPCD step.
+//
+// One launch of step_kernel completes step k of every box: for each cell it
+// stages the cell's bucket in shared memory with bulk (TMA) copies, streams the
+// particles (step k), collides them (SRD or extended MPC), undoes the grid
+// shift, accumulates the lab-grid sample if asked, streams each particle again
+// for step k+1 only to find its next cell, and scatters the post-collision
+// state into that cell's bucket of the other parity.  Particles are therefore
+// stored post-collision (the state the reference exposes between steps) and
+// keyed by their next cell; streaming is recomputed, bit-identically, where it
+// is needed.
+//
+// Reference path being replaced: translateParticles (simulation_kernels.cu:65-143),
+// srdCollision (srd_collision_strategy.cu:12-157), ext::fusedCollision
+// (extended_collision_strategy.cu:17-332), the counting sort (sort_particles.cu)
+// and the sampling kernels (simulation_kernels.cu:150-230); the arithmetic
+// follows the CPU backend (cpu_backend/simulation_functions.cpp:38-406).
+#include <cstdio>
+
+#include "mpcd_device.cuh"
+#include "mpcd_kernels.h"
+
+namespace mpcd_gb {
+
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr uint64_t kWaitLimitNs = 2000000000ull;   // 2 s bound on any wait
+
+__device__ __forceinline__ uint64_t globaltimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Wait for the phase with the given parity; false after kWaitLimitNs.
+__device__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer();
+    while (true) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (globaltimer() - t0 > kWaitLimitNs) return false;
+    }
+}
+
+// Bulk copy global -> shared (16-byte aligned, size a multiple of 16), completing on bar.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Exclusive scan of one value per thread (blockDim == kThreads), total returned.
+__device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_tot, uint32_t& total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < kThreads / 32 ? warp_tot[lane] : 0u;
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(kFull, wi, o);
+            if (lane >= o) wi += t;
+        }
+        if (lane < kThreads / 32) warp_tot[lane] = wi - w;
+        if (lane == kThreads / 32 - 1) warp_tot[kThreads / 32] = wi;
+    }
+    __syncthreads();
+    const uint32_t excl = incl - v + warp_tot[warp];
+    total = warp_tot[kThreads / 32];
+    __syncthreads();
+    return excl;
+}
+
+__device__ __forceinline__ const BoxDesc* find_box(const StepArgs& a, uint32_t tile, int& index)
+{
+    int lo = 0, hi = a.nboxes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.boxes[mid].tile_base <= tile) lo = mid; else hi = mid - 1;
+    }
+    index = lo;
+    return &a.boxes[lo];
+}
+
+__device__ __forceinline__ int box_of_particle(const BoxDesc* boxes, int nboxes, uint64_t id)
+{
+    int lo = 0, hi = nboxes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (boxes[mid].dense_base <= id) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Claim a slot in `count[key]` for every active lane; lanes that share a key
+// are served by one atomic (warp-aggregated).  Returns the slot.
+__device__ __forceinline__ uint32_t claim_slot(uint32_t* count, uint64_t key, bool active)
+{
+    const unsigned act = __ballot_sync(kFull, active);
+    uint32_t slot = 0;
+    if (active) {
+        const unsigned peers = __match_any_sync(act, key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if ((int)(threadIdx.x & 31) == leader) base = atomicAdd(count + key, (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        slot = base + (uint32_t)__popc(peers & lanemask_lt());
+    }
+    return slot;
+}
+
+// Accumulate (v, 1) into samp[lab] for every active lane, one atomic per distinct cell per warp.
+__device__ __forceinline__ void sample_add(float4* samp, uint64_t lab, float3 v, bool active)
+{
+    unsigned todo = __ballot_sync(kFull, active);
+    while (todo) {
+        const int leader = __ffs(todo) - 1;
+        const uint64_t key = __shfl_sync(kFull, lab, leader);
+        const bool mine = active && ((todo >> (threadIdx.x & 31)) & 1u) && lab == key;
+        const unsigned grp = __ballot_sync(kFull, mine);
+        float sx = mine ? v.x : 0.0f, sy = mine ? v.y : 0.0f, sz = mine ? v.z : 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sx += __shfl_xor_sync(kFull, sx, o);
+            sy += __shfl_xor_sync(kFull, sy, o);
+            sz += __shfl_xor_sync(kFull, sz, o);
+        }
+        if ((int)(threadIdx.x & 31) == leader) atomicAdd(samp + key, make_float4(sx, sy, sz, (float)__popc(grp)));
+        todo &= ~grp;
+    }
+}
+
+// Write one post-collision particle into its next bucket, or into the overflow list.
+__device__ __forceinline__ void scatter_particle(const StepArgs& a, const BoxDesc& b, float3 x, float3 v,
+                                                 uint32_t prev, uint32_t id, float3 next_shift, bool active)
+{
+    uint64_t key = 0;
+    if (active) {
+        float3 vn = v;
+        const float3 xn = stream_shift(b, x, vn, next_shift);
+        key = (uint64_t)b.cell_base + storage_index(b, cell_of(b, xn));
+    }
+    const uint32_t slot = claim_slot(a.out_count, key, active);
+    if (!active) return;
+    if (slot < b.cap) {
+        const uint64_t at = b.slot_base + (key - b.cell_base) * (uint64_t)b.cap + slot;
+        a.out_pos[at] = make_float4(x.x, x.y, x.z, __uint_as_float(prev));
+        a.out_vel[at] = make_float4(v.x, v.y, v.z, __uint_as_float(id));
+    } else {
+        atomicAdd(&a.state->overflow_total, 1ull);
+        const unsigned parity = (unsigned)((a.step + 1) & 1);
+        const unsigned q = atomicAdd(&a.state->ov_count[parity], 1u);
+        if (q < a.ov_cap) {
+            a.ov_out_pos[q] = make_float4(x.x, x.y, x.z, __uint_as_float(prev));
+            a.ov_out_vel[q] = make_float4(v.x, v.y, v.z, __uint_as_float(id));
+        } else {
+            atomicOr(&a.state->error_flags, kErrOverflowListFull);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ draws
+
+template <bool TABLE>
+struct Draws;
+
+template <>
+struct Draws<false> {   // Philox (production)
+    __device__ static uint32_t ghost_count(const StepArgs&, const BoxDesc& b, uint64_t step, uint32_t ref,
+                                           float shift, bool layer, bool sign)
+    {
+        uint32_t g = 0;
+        uint4 o = make_uint4(0, 0, 0, 0);
+        for (uint32_t i = 0; i < b.n; ++i) {
+            if ((i & 3u) == 0) o = draw(b, step, kGhostCount, ref, i >> 2);
+            const uint32_t u = (i & 3u) == 0 ? o.x : (i & 3u) == 1 ? o.y : (i & 3u) == 2 ? o.z : o.w;
+            if ((u01(u) > shift) ^ layer ^ sign) ++g;
+        }
+        return g;
+    }
+    __device__ static void ghost(const StepArgs&, const BoxDesc& b, uint64_t step, uint32_t ref, uint32_t j,
+                                 float3 centre, float shift, bool layer, bool sign, float3& x, float3& v)
+    {
+        uint4 o = draw(b, step, kGhost, ref, 2 * j);
+        const float uz = u01(o.z);
+        const float z = (layer ^ sign) ? shift * uz : shift + (1.0f - shift) * uz;
+        x = make_float3((u01(o.x) - 0.5f) + centre.x, (u01(o.y) - 0.5f) + centre.y, (z - 0.5f) + centre.z);
+        o = draw(b, step, kGhost, ref, 2 * j + 1);
+        float g0, g1, g2, g3;
+        box_muller(o.x, o.y, g0, g1);
+        box_muller(o.z, o.w, g2, g3);
+        v = make_float3(g0 * b.tv, g1 * b.tv, g2 * b.tv);
+    }
+    __device__ static float3 srd_axis(const StepArgs&, const BoxDesc& b, uint64_t step, uint32_t ref)
+    {
+        const uint4 o = draw(b, step, kAxis, ref, 0);
+        const float z = 1.0f - 2.0f * u01(o.x);
+        const float rho = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+        float s, c;
+        sincospif(2.0f * u01(o.y), &s, &c);
+        return make_float3(rho * c, rho * s, z);
+    }
+    __device__ static float3 ext_axis(const StepArgs& a, const BoxDesc& b, uint64_t step, uint32_t ref, float& gate)
+    {
+        const uint4 o = draw(b, step, kAxis, ref, 0);
+        const uint32_t sel = (o.x >> 1) % 13u;
+        float3 ax = make_float3(a.ext_axis[sel][0], a.ext_axis[sel][1], a.ext_axis[sel][2]);
+        if ((o.y >> 1) & 1u) ax = make_float3(-ax.x, -ax.y, -ax.z);
+        gate = u01(o.z);
+        return ax;
+    }
+    __device__ static float thermal(const StepArgs&, const BoxDesc& b, uint64_t step, uint32_t ref, uint32_t i)
+    {
+        const uint4 o = draw(b, step, kThermal, ref, i >> 2);
+        float g0, g1;
+        if (((i & 3u) >> 1) == 0) box_muller(o.x, o.y, g0, g1);
+        else box_muller(o.z, o.w, g0, g1);
+        return (i & 1u) ? g1 : g0;
+    }
+};
+
+template <>
+struct Draws<true> {    // injected tables (test hook)
+    __device__ static uint32_t ghost_count(const StepArgs& a, const BoxDesc&, uint64_t, uint32_t ref, float, bool,
+                                           bool)
+    {
+        return a.draws.ghost_count[ref];
+    }
+    __device__ static void ghost(const StepArgs& a, const BoxDesc&, uint64_t, uint32_t ref, uint32_t j, float3,
+                                 float, bool, bool, float3& x, float3& v)
+    {
+        const float* p = a.draws.ghost_pos + ((size_t)ref * a.draws.gmax + j) * 3;
+        const float* q = a.draws.ghost_vel + ((size_t)ref * a.draws.gmax + j) * 3;
+        x = make_float3(p[0], p[1], p[2]);
+        v = make_float3(q[0], q[1], q[2]);
+    }
+    __device__ static float3 srd_axis(const StepArgs& a, const BoxDesc&, uint64_t, uint32_t ref)
+    {
+        const float* p = a.draws.axis + (size_t)ref * 3;
+        return make_float3(p[0], p[1], p[2]);
+    }
+    __device__ static float3 ext_axis(const StepArgs& a, const BoxDesc&, uint64_t, uint32_t ref, float& gate)
+    {
+        const float* p = a.draws.axis + (size_t)ref * 3;
+        gate = a.draws.gate_u[ref];
+        return make_float3(p[0], p[1], p[2]);
+    }
+    __device__ static float thermal(const StepArgs& a, const BoxDesc&, uint64_t, uint32_t ref, uint32_t i)
+    {
+        return a.draws.gauss[(size_t)ref * a.draws.pmax + i];
+    }
+};
+
+// SymmetricMatrix::inverse(tolerance) (common/mechanic.hpp:52-79); m = {xx,yy,zz,xy,xz,yz}
+__device__ __forceinline__ void sym_inverse(const float m[6], float tol, float o[6])
+{
+    const float xx = m[0], yy = m[1], zz = m[2], xy = m[3], xz = m[4], yz = m[5];
+    float det = xx * (yy * zz - yz * yz) + xz * (2 * xy * yz - yy * xz) - (xy * xy * zz);
+    if (det < 0) det = 0;
+    if (det > tol) {
+        const float inv = 1 / det;
+        o[0] = (yy * zz - yz * yz) * inv;
+        o[1] = (xx * zz - xz * xz) * inv;
+        o[2] = (xx * yy - xy * xy) * inv;
+        o[3] = (xz * yz - zz * xy) * inv;
+        o[4] = (xy * yz - yy * xz) * inv;
+        o[5] = (xy * xz - xx * yz) * inv;
+    } else {
+        const float tr = xx + yy + zz;
+        if (tr > tol) {
+            const float s = 4 / (tr * tr);
+            for (int k = 0; k < 6; ++k) o[k] = m[k] * s;
+        } else {
+            for (int k = 0; k < 6; ++k) o[k] = 0.0f;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ step kernel
+
+struct TileShared {
+    uint32_t cnt[kMaxTileCells];       // real particles staged per cell
+    uint32_t ng[kMaxTileCells];        // ghosts per cell
+    uint32_t off[kMaxTileCells + 1];   // particle offset (real + ghosts) per cell, tile-relative
+    uint32_t goff[kMaxTileCells + 1];  // ghost offset per cell
+    float4 c0[kMaxTileCells];          // SRD: mean, n in w | EXT: mean
+    float4 c1[kMaxTileCells];          // SRD: axis        | EXT: centre of mass
+    float4 c2[kMaxTileCells];          // EXT: omega, participants in w
+    uint32_t warp_tot[kThreads / 32 + 1];
+    uint32_t ov_n;
+    uint32_t abort;
+    uint64_t bar;
+};
+
+// Overflow particles of step k (they found their bucket full when step k-1
+// scattered them): as in the reference, they stream but skip the collision,
+// and keep the unshifted position pbc(pbc(x + s) - s) (simulation_functions.cpp:90-93).
+__device__ void overflow_pass(const StepArgs& a, TileShared& sh)
+{
+    const unsigned parity = (unsigned)(a.step & 1);
+    if (threadIdx.x == 0) sh.ov_n = min(a.state->ov_count[parity], a.ov_cap);
+    __syncthreads();
+    const uint32_t n = sh.ov_n;
+    for (uint32_t base = 0; base < n; base += kThreads) {
+        const uint32_t q = base + threadIdx.x;
+        const bool active = q < n;
+        int bi = 0;
+        uint32_t id = 0;
+        float3 x = make_float3(0, 0, 0), v = make_float3(0, 0, 0);
+        float3 sn = make_float3(0, 0, 0);
+        if (active) {
+            const float4 p = a.ov_in_pos[q], w = a.ov_in_vel[q];
+            id = __float_as_uint(w.w);
+            bi = box_of_particle(a.boxes, a.nboxes, id);
+            const BoxDesc& b = a.boxes[bi];
+            x = make_float3(p.x, p.y, p.z);
+            v = make_float3(w.x, w.y, w.z);
+            const float3 s = grid_shift(b, bi, a.step, a.state);
+            const float3 xs = stream_shift(b, x, v, s);
+            x = pbc(b, make_float3(xs.x - s.x, xs.y - s.y, xs.z - s.z));
+            sn = grid_shift(b, bi, a.step + 1, a.state);
+        }
+        const BoxDesc& b = a.boxes[bi];
+        if (a.sample) {
+            const uint64_t lab = active ? (uint64_t)b.cell_base + ref_index(b, cell_of(b, x)) : 0;
+            sample_add(a.samp, lab, v, active);
+        }
+        scatter_particle(a, b, x, v, (uint32_t)(a.total_slots + q), id, sn, active);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) a.state->ov_count[parity] = 0;
+}
+
+template <int ALGO, bool TABLE>
+__global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32_t pbuf)
+{
+    using D = Draws<TABLE>;
+    extern __shared__ __align__(128) unsigned char dyn[];
+    __shared__ TileShared sh;
+    float4* s_pos = reinterpret_cast<float4*>(dyn);
+    float4* s_vel = s_pos + pbuf;
+    uint16_t* s_cell = reinterpret_cast<uint16_t*>(s_vel + pbuf);
+    uint16_t* s_inv = s_cell + pbuf;
+    uint16_t* s_rank = s_inv + pbuf;
+    __shared__ BoxDesc sbox;
+    __shared__ int sbox_index;
+    __shared__ float3 sshift[2];
+
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&sh.bar);
+        sh.abort = 0;
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+
+    if (blockIdx.x == 0) overflow_pass(a, sh);
+
+    for (uint32_t tile = blockIdx.x; tile < a.num_tiles; tile += gridDim.x) {
+        if (tid == 0) {
+            int bi;
+            const BoxDesc* bp = find_box(a, tile, bi);
+            sbox = *bp;
+            sbox_index = bi;
+            sshift[0] = grid_shift(*bp, bi, a.step, a.state);
+            sshift[1] = grid_shift(*bp, bi, a.step + 1, a.state);
+        }
+        __syncthreads();
+        const BoxDesc& b = sbox;
+        const int bi = sbox_index;
+        const uint32_t c0 = (tile - b.tile_base) * b.tile_cells;
+        const uint32_t nc = min(b.tile_cells, b.C - c0);
+        const float3 s = sshift[0];
+        const float3 sn = sshift[1];
+        const float shift_abs = fabsf(s.z);
+        const bool sign = s.z > 0;
+
+        // phase 0: counts (zeroed for reuse two steps later) and ghost counts
+        uint32_t mine = 0, mine_g = 0;
+        if (tid < (int)nc) {
+            const uint32_t g = b.cell_base + c0 + tid;
+            const uint32_t raw = a.in_count[g];
+            a.in_count[g] = 0;
+            mine = min(raw, b.cap);
+            const uint3 cc = storage_coords(b, c0 + tid);
+            bool layer, ghosts;
+            wall_layer(b, cc.z, sign, layer, ghosts);
+            if (ghosts) mine_g = D::ghost_count(a, b, a.step, ref_index(b, cc), shift_abs, layer, sign);
+            sh.cnt[tid] = mine;
+            sh.ng[tid] = mine_g;
+        }
+        uint32_t total;
+        const uint32_t off = block_exclusive_scan(mine + mine_g, sh.warp_tot, total);
+        uint32_t gtotal;
+        const uint32_t goff = block_exclusive_scan(mine_g, sh.warp_tot, gtotal);
+        if (tid < (int)nc) {
+            sh.off[tid] = off;
+            sh.goff[tid] = goff;
+        }
+        if (tid == 0) {
+            sh.off[nc] = total;
+            sh.goff[nc] = gtotal;
+        }
+        __syncthreads();
+
+        // sub-tiles of consecutive cells whose particles fit the buffer
+        uint32_t i0 = 0;
+        while (i0 < nc) {
+            uint32_t lo = i0 + 1, hi = nc;   // largest i1 with off[i1] - off[i0] <= pbuf
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (sh.off[mid] - sh.off[i0] <= pbuf) lo = mid; else hi = mid - 1;
+            }
+            const uint32_t i1 = lo;
+            const uint32_t pbase = sh.off[i0];
+            const uint32_t np = sh.off[i1] - pbase;
+            if (np > pbuf) {   // impossible while 5n <= pbuf (checked on the host)
+                if (tid == 0) atomicOr(&a.state->error_flags, kErrKeyMismatch);
+                return;
+            }
+
+            // stage real particles: one bulk copy per cell and array
+            uint32_t real_bytes = 0;
+            for (uint32_t i = i0; i < i1; ++i) real_bytes += sh.cnt[i];   // all threads, smem broadcast
+            real_bytes *= 32u;
+            if (tid == 0 && real_bytes) {
+                fence_proxy_async();
+                mbar_arrive_expect_tx(&sh.bar, real_bytes);
+            }
+            __syncthreads();
+            for (uint32_t i = i0 + tid; i < i1; i += kThreads) {
+                const uint32_t n = sh.cnt[i];
+                if (n) {
+                    fence_proxy_async();
+                    const uint64_t src = b.slot_base + (uint64_t)(c0 + i) * b.cap;
+                    const uint32_t dst = sh.off[i] - pbase;
+                    bulk_g2s(s_pos + dst, a.in_pos + src, n * 16u, &sh.bar);
+                    bulk_g2s(s_vel + dst, a.in_vel + src, n * 16u, &sh.bar);
+                }
+                // tile-local cell id of every staged particle, ghosts included
+                const uint32_t o = sh.off[i] - pbase, e = sh.off[i + 1] - pbase;
+                for (uint32_t p = o; p < e; ++p) s_cell[p] = (uint16_t)i;
+            }
+            // ghosts, one thread per ghost (overlaps the copies)
+            {
+                const uint32_t gb = sh.goff[i0], ge = sh.goff[i1];
+                for (uint32_t q = gb + tid; q < ge; q += kThreads) {
+                    uint32_t lo2 = i0, hi2 = i1 - 1;   // cell with goff[i] <= q < goff[i+1]
+                    while (lo2 < hi2) {
+                        const uint32_t mid = (lo2 + hi2 + 1) >> 1;
+                        if (sh.goff[mid] <= q) lo2 = mid; else hi2 = mid - 1;
+                    }
+                    const uint32_t i = lo2, j = q - sh.goff[i];
+                    const uint3 cc = storage_coords(b, c0 + i);
+                    bool layer, ghosts;
+                    wall_layer(b, cc.z, sign, layer, ghosts);
+                    float3 gx, gv;
+                    D::ghost(a, b, a.step, ref_index(b, cc), j, cell_centre(b, cc), shift_abs, layer, sign, gx, gv);
+                    const uint32_t p = sh.off[i] - pbase + sh.cnt[i] + j;
+                    s_pos[p] = make_float4(gx.x, gx.y, gx.z, 0.0f);
+                    s_vel[p] = make_float4(gv.x, gv.y, gv.z, 0.0f);
+                }
+            }
+            if (real_bytes) {
+                int ok = 1;
+                if (tid == 0) ok = mbar_wait_bounded(&sh.bar, phase);
+                ok = __syncthreads_and(ok);
+                if (!ok) {
+                    if (tid == 0) {
+                        atomicOr(&a.state->error_flags, kErrWaitTimeout);
+                        mbar_wait_bounded(&sh.bar, phase);   // let copies in flight land
+                    }
+                    return;
+                }
+                mbar_try_wait(&sh.bar, phase);   // completed phase: acquire for every thread
+                phase ^= 1u;
+            } else {
+                __syncthreads();
+            }
+
+            // phase 3: stream step k (recomputed) and stable rank by prev key
+            for (uint32_t p = tid; p < np; p += kThreads) {
+                const uint32_t i = s_cell[p];
+                const uint32_t o = sh.off[i] - pbase;
+                const uint32_t r = p - o;
+                if (r < sh.cnt[i]) {
+                    const float4 xp = s_pos[p], vp = s_vel[p];
+                    float3 x = make_float3(xp.x, xp.y, xp.z), v = make_float3(vp.x, vp.y, vp.z);
+                    x = stream_shift(b, x, v, s);
+                    const uint32_t key = __float_as_uint(xp.w);
+                    uint32_t rank = 0;   // ties (never expected) broken by staging order: always a permutation
+                    for (uint32_t q = 0; q < sh.cnt[i]; ++q) {
+                        const uint32_t kq = __float_as_uint(s_pos[o + q].w);
+                        rank += kq < key || (kq == key && q < r);
+                    }
+                    if (storage_index(b, cell_of(b, x)) != c0 + i) atomicOr(&a.state->error_flags, kErrKeyMismatch);
+                    s_rank[p] = (uint16_t)rank;
+                    s_inv[o + rank] = (uint16_t)p;
+                    s_vel[p] = make_float4(v.x, v.y, v.z, vp.w);
+                    s_pos[p].x = x.x;
+                    s_pos[p].y = x.y;
+                    s_pos[p].z = x.z;
+                }
+            }
+            __syncthreads();
+
+            // phase 5: one thread per cell
+            for (uint32_t i = i0 + tid; i < i1; i += kThreads) {
+                const uint32_t o = sh.off[i] - pbase, cnt = sh.cnt[i], g = sh.ng[i];
+                const uint3 cc = storage_coords(b, c0 + i);
+                const uint32_t ref = ref_index(b, cc);
+                if (ALGO == 0) {
+                    const uint32_t n = cnt + g;
+                    float3 mean = make_float3(0, 0, 0), axis = make_float3(0, 0, 0);
+                    if (n > 1) {
+                        for (uint32_t r = 0; r < cnt; ++r) {
+                            const float4 w = s_vel[s_inv[o + r]];
+                            mean.x += w.x; mean.y += w.y; mean.z += w.z;
+                        }
+                        for (uint32_t j = 0; j < g; ++j) {
+                            const float4 w = s_vel[o + cnt + j];
+                            mean.x += w.x; mean.y += w.y; mean.z += w.z;
+                        }
+                        const float inv = 1.0f / (float)n;
+                        mean.x *= inv; mean.y *= inv; mean.z *= inv;
+                        axis = D::srd_axis(a, b, a.step, ref);
+                    }
+                    sh.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));
+                    sh.c1[i] = make_float4(axis.x, axis.y, axis.z, 0.0f);
+                } else {
+                    const uint32_t n = min(cnt + g, b.cap);
+                    const uint32_t m = n - g;   // real participants (leading ranks)
+                    float3 com = make_float3(0, 0, 0), mean = make_float3(0, 0, 0), omega = make_float3(0, 0, 0);
+                    if (n > 1) {
+                        const float3 centre = cell_centre(b, cc);
+                        float gate;
+                        const float3 axis = D::ext_axis(a, b, a.step, ref, gate);
+                        auto at = [&](uint32_t k) -> uint32_t { return k < m ? s_inv[o + k] : o + cnt + (k - m); };
+                        for (uint32_t k = 0; k < n; ++k) {
+                            const uint32_t p = at(k);
+                            const float4 xp = s_pos[p], vp = s_vel[p];
+                            com.x += (xp.x - centre.x); com.y += (xp.y - centre.y); com.z += (xp.z - centre.z);
+                            mean.x += vp.x; mean.y += vp.y; mean.z += vp.z;
+                        }
+                        const float inv = 1.0f / (float)n;
+                        com = make_float3(com.x * inv + centre.x, com.y * inv + centre.y, com.z * inv + centre.z);
+                        mean = make_float3(mean.x * inv, mean.y * inv, mean.z * inv);
+                        float proj0 = 0.0f;
+                        int size0 = 0;
+                        for (uint32_t k = 0; k < n; ++k) {
+                            const uint32_t p = at(k);
+                            float4 xp = s_pos[p], vp = s_vel[p];
+                            xp.x -= com.x; xp.y -= com.y; xp.z -= com.z;
+                            vp.x -= mean.x; vp.y -= mean.y; vp.z -= mean.z;
+                            s_pos[p] = xp;
+                            s_vel[p] = vp;
+                            if (dot3(make_float3(xp.x, xp.y, xp.z), axis) < 0) {
+                                proj0 += dot3(make_float3(vp.x, vp.y, vp.z), axis);
+                                size0 += 1;
+                            }
+                        }
+                        const int size1 = (int)n - size0;
+                        const float proj1 = -proj0 / (float)size1;
+                        proj0 = proj0 / (float)size0;
+                        const float prob = 1 - expf(0.01f * (proj1 - proj0) * (float)size0 * (float)size1);
+                        if (gate < prob) {
+                            const float t0 = proj1 * ((float)size1 / (float)size0);
+                            const float t1 = proj0 * ((float)size0 / (float)size1);
+                            float mean0 = 0.0f, mean1 = 0.0f;
+                            float I[6] = {0, 0, 0, 0, 0, 0};
+                            float3 dL = make_float3(0, 0, 0);
+                            for (uint32_t k = 0; k < n; ++k) {
+                                const uint32_t p = at(k);
+                                const float4 xp = s_pos[p];
+                                float4 vp = s_vel[p];
+                                const float3 x = make_float3(xp.x, xp.y, xp.z);
+                                float3 v = make_float3(vp.x, vp.y, vp.z);
+                                const bool side = dot3(x, axis) < 0;
+                                const float vr = D::thermal(a, b, a.step, ref, k) * b.tv;
+                                if (side) mean0 += vr; else mean1 += vr;
+                                const float3 cr = cross3(x, v);
+                                dL.x += cr.x; dL.y += cr.y; dL.z += cr.z;
+                                const float kick = (vr - dot3(v, axis)) + (side ? t0 : t1);
+                                v.x += axis.x * kick; v.y += axis.y * kick; v.z += axis.z * kick;
+                                s_vel[p] = make_float4(v.x, v.y, v.z, vp.w);
+                                const float sx = x.x * x.x, sy = x.y * x.y, sz = x.z * x.z;
+                                I[0] += sy + sz;
+                                I[1] += sx + sz;
+                                I[2] += sx + sy;
+                                I[3] += -x.x * x.y;
+                                I[4] += -x.x * x.z;
+                                I[5] += -x.y * x.z;
+                            }
+                            const float m0 = mean0 / (float)size0, m1 = mean1 / (float)size1;
+                            const float3 vm0 = make_float3(axis.x * m0, axis.y * m0, axis.z * m0);
+                            const float3 vm1 = make_float3(axis.x * m1, axis.y * m1, axis.z * m1);
+                            for (uint32_t k = 0; k < n; ++k) {
+                                const uint32_t p = at(k);
+                                const float4 xp = s_pos[p];
+                                float4 vp = s_vel[p];
+                                const float3 x = make_float3(xp.x, xp.y, xp.z);
+                                const float3 vm = dot3(x, axis) < 0 ? vm0 : vm1;
+                                vp.x -= vm.x; vp.y -= vm.y; vp.z -= vm.z;
+                                s_vel[p] = vp;
+                                const float3 cr = cross3(x, make_float3(vp.x, vp.y, vp.z));
+                                dL.x -= cr.x; dL.y -= cr.y; dL.z -= cr.z;
+                            }
+                            float Ii[6];
+                            sym_inverse(I, 1e-5f, Ii);
+                            omega = make_float3(Ii[0] * dL.x + Ii[3] * dL.y + Ii[4] * dL.z,
+                                                Ii[3] * dL.x + Ii[1] * dL.y + Ii[5] * dL.z,
+                                                Ii[4] * dL.x + Ii[5] * dL.y + Ii[2] * dL.z);
+                        }
+                    }
+                    sh.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));
+                    sh.c1[i] = make_float4(com.x, com.y, com.z, 0.0f);
+                    sh.c2[i] = make_float4(omega.x, omega.y, omega.z, __uint_as_float(m));
+                }
+            }
+            __syncthreads();
+
+            // phase 6: one thread per real particle: finish, sample, scatter
+            for (uint32_t base = 0; base < np; base += kThreads) {
+                const uint32_t p = base + tid;
+                bool active = false;
+                uint32_t i = 0, r = 0;
+                if (p < np) {
+                    i = s_cell[p];
+                    r = p - (sh.off[i] - pbase);
+                    active = r < sh.cnt[i];
+                }
+                float3 x = make_float3(0, 0, 0), v = make_float3(0, 0, 0);
+                uint32_t prev = 0, id = 0;
+                if (active) {
+                    const float4 xp = s_pos[p], vp = s_vel[p];
+                    x = make_float3(xp.x, xp.y, xp.z);
+                    v = make_float3(vp.x, vp.y, vp.z);
+                    id = __float_as_uint(vp.w);
+                    const uint32_t rank = s_rank[p];
+                    prev = (uint32_t)(b.slot_base + (uint64_t)(c0 + i) * b.cap + rank);
+                    const float4 k0 = sh.c0[i], k1 = sh.c1[i];
+                    const uint32_t n = __float_as_uint(k0.w);
+                    const float3 mean = make_float3(k0.x, k0.y, k0.z);
+                    if (ALGO == 0) {
+                        if (n > 1) {
+                            const float3 axis = make_float3(k1.x, k1.y, k1.z);
+                            const float3 vr = make_float3(v.x - mean.x, v.y - mean.y, v.z - mean.z);
+                            const float vd = dot3(vr, axis);
+                            const float3 vpara = make_float3(axis.x * vd, axis.y * vd, axis.z * vd);
+                            const float3 vperp = make_float3(vr.x - vpara.x, vr.y - vpara.y, vr.z - vpara.z);
+                            const float3 cr = cross3(vperp, axis);
+                            v = make_float3((vpara.x + b.cos_a * vperp.x) + b.sin_a * cr.x,
+                                            (vpara.y + b.cos_a * vperp.y) + b.sin_a * cr.y,
+                                            (vpara.z + b.cos_a * vperp.z) + b.sin_a * cr.z);
+                            v.x += mean.x; v.y += mean.y; v.z += mean.z;
+                            x = pbc(b, make_float3(x.x - s.x, x.y - s.y, x.z - s.z));
+                            v.x += b.drag_dt;
+                        }
+                    } else {
+                        const float4 k2 = sh.c2[i];
+                        const uint32_t m = __float_as_uint(k2.w);
+                        if (n > 1 && rank < m) {
+                            const float3 com = make_float3(k1.x, k1.y, k1.z);
+                            const float3 omega = make_float3(k2.x, k2.y, k2.z);
+                            v.x += mean.x; v.y += mean.y; v.z += mean.z;
+                            v.x += b.drag_dt;
+                            const float3 cr = cross3(x, omega);
+                            v.x -= cr.x; v.y -= cr.y; v.z -= cr.z;
+                            x = pbc(b, make_float3((com.x + x.x) - s.x, (com.y + x.y) - s.y, (com.z + x.z) - s.z));
+                        }
+                    }
+                }
+                if (a.sample) {
+                    const uint64_t lab = active ? (uint64_t)b.cell_base + ref_index(b, cell_of(b, x)) : 0;
+                    sample_add(a.samp, lab, v, active);
+                }
+                scatter_particle(a, b, x, v, prev, id, sn, active);
+            }
+            __syncthreads();
+            i0 = i1;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ prologue scatter
+
+// Key dense clean particles by their cell after streaming step k and scatter them
+// into the buckets of parity k; particle id = prev = dense index.  The launch
+// plays the epilogue of step k-1: a.step = k - 1, a.out_* = buckets of parity k.
+__global__ void __launch_bounds__(kThreads) scatter_kernel(StepArgs a, const float* pos, const float* vel,
+                                                           uint64_t n_total)
+{
+    for (uint64_t base = (uint64_t)blockIdx.x * kThreads; base < n_total; base += (uint64_t)gridDim.x * kThreads) {
+        const uint64_t i = base + threadIdx.x;
+        const bool active = i < n_total;
+        int bi = 0;
+        float3 x = make_float3(0, 0, 0), v = make_float3(0, 0, 0);
+        float3 s = make_float3(0, 0, 0);
+        if (active) {
+            bi = box_of_particle(a.boxes, a.nboxes, i);
+            x = make_float3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+            v = make_float3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+            s = grid_shift(a.boxes[bi], bi, a.step + 1, a.state);
+        }
+        scatter_particle(a, a.boxes[bi], x, v, (uint32_t)i, (uint32_t)i, s, active);
+    }
+}
+
+// ------------------------------------------------------------------ sampling
+
+// Per lab cell: mean velocity of the step (0 for an empty cell, as averageReduceOnly)
+// into the FP64 running sums; snapshot or accumulate (cpu_backend.cpp:189-211).
+__global__ void sample_finalize_kernel(float4* samp, SampleAcc* acc, uint64_t cells, int snapshot)
+{
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells;
+         c += (uint64_t)gridDim.x * blockDim.x) {
+        const float4 s = samp[c];
+        float mx = s.x, my = s.y, mz = s.z;
+        if (s.w > 0.0f) {
+            const float inv = 1.0f / s.w;
+            mx *= inv; my *= inv; mz *= inv;
+        }
+        SampleAcc r = snapshot ? SampleAcc{0, 0, 0, 0} : acc[c];
+        r.n += (double)s.w;
+        r.vx += (double)mx;
+        r.vy += (double)my;
+        r.vz += (double)mz;
+        acc[c] = r;
+        samp[c] = make_float4(0, 0, 0, 0);
+    }
+}
+
+// ------------------------------------------------------------------ compaction
+
+// Decoupled look-back exclusive scan of min(count, cap) over all cells
+// (Merrill & Garland, "Single-pass parallel prefix scan with decoupled look-back").
+// status[t]: bits 62-63 flag (1 aggregate, 2 inclusive prefix), low 32 value.
+constexpr int kScanItems = 8;
+constexpr uint64_t kFlagAgg = 1ull << 62, kFlagPre = 2ull << 62;
+
+__device__ __forceinline__ uint32_t cell_cap(const BoxDesc* boxes, int nboxes, uint64_t c)
+{
+    int lo = 0, hi = nboxes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (boxes[mid].cell_base <= c) lo = mid; else hi = mid - 1;
+    }
+    return boxes[lo].cap;
+}
+
+__global__ void __launch_bounds__(kThreads) scan_kernel(const uint32_t* count, const BoxDesc* boxes, int nboxes,
+                                                        uint64_t cells, uint32_t* offsets,
+                                                        unsigned long long* status, unsigned int* tile_counter,
+                                                        DeviceState* state)
+{
+    __shared__ uint32_t warp_tot[kThreads / 32 + 1];
+    __shared__ uint32_t s_tile, s_prefix;
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t first = (uint64_t)tile * kThreads * kScanItems + (uint64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems], sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const uint64_t c = first + k;
+        v[k] = c < cells ? min(count[c], cell_cap(boxes, nboxes, c)) : 0u;
+        sum += v[k];
+    }
+    uint32_t total;
+    const uint32_t excl = block_exclusive_scan(sum, warp_tot, total);
+    if (threadIdx.x == 0) {
+        uint32_t prefix = 0;
+        if (tile == 0) {
+            atomicExch(status + tile, kFlagPre | total);
+        } else {
+            atomicExch(status + tile, kFlagAgg | total);
+            int64_t t = (int64_t)tile - 1;
+            const uint64_t t0 = globaltimer();
+            bool timed_out = false;
+            while (t >= 0) {
+                const unsigned long long w = atomicAdd(status + t, 0ull);
+                const uint64_t flag = w & (3ull << 62);
+                if (flag == 0) {
+                    if (globaltimer() - t0 > kWaitLimitNs) { timed_out = true; break; }
+                    continue;
+                }
+                prefix += (uint32_t)w;
+                if (flag == kFlagPre) break;
+                --t;
+            }
+            if (timed_out) atomicOr(&state->error_flags, kErrWaitTimeout);
+            atomicExch(status + tile, kFlagPre | (uint32_t)(prefix + total));
+        }
+        s_prefix = prefix;
+    }
+    __syncthreads();
+    uint32_t run = s_prefix + excl;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const uint64_t c = first + k;
+        if (c < cells) offsets[c] = run;
+        run += v[k];
+    }
+    if (tile == (uint32_t)((cells + kThreads * kScanItems - 1) / (kThreads * kScanItems)) - 1 &&
+        threadIdx.x == kThreads - 1)
+        offsets[cells] = s_prefix + total;
+}
+
+// Layout dump: the particles of every cell, in stable order, cells in storage
+// order, followed by the overflow list.  offsets from scan_kernel.
+__global__ void __launch_bounds__(kThreads) compact_kernel(const StepArgs a, const uint32_t* count,
+                                                           const float4* pos, const float4* vel,
+                                                           const uint32_t* offsets, uint64_t cells, uint64_t n_total,
+                                                           uint32_t* out_cell, uint32_t* out_slot, uint32_t* out_prev,
+                                                           uint32_t* out_id)
+{
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells;
+         c += (uint64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = a.nboxes - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a.boxes[mid].cell_base <= c) lo = mid; else hi = mid - 1;
+        }
+        const BoxDesc& b = a.boxes[lo];
+        const uint32_t n = min(count[c], b.cap);
+        const uint64_t slot0 = b.slot_base + (c - b.cell_base) * b.cap;
+        const uint32_t dst0 = offsets[c];
+        const uint32_t ref = ref_index(b, storage_coords(b, (uint32_t)(c - b.cell_base)));
+        for (uint32_t q = 0; q < n; ++q) {
+            const uint32_t key = __float_as_uint(pos[slot0 + q].w);
+            uint32_t rank = 0;
+            for (uint32_t u = 0; u < n; ++u) {
+                const uint32_t ku = __float_as_uint(pos[slot0 + u].w);
+                rank += ku < key || (ku == key && u < q);
+            }
+            const uint64_t d = (uint64_t)dst0 + rank;
+            if (d >= n_total) {
+                atomicOr(&a.state->error_flags, kErrKeyMismatch);
+                continue;
+            }
+            if (out_cell) out_cell[d] = b.cell_base + ref;
+            if (out_slot) out_slot[d] = (uint32_t)(slot0 + rank);
+            if (out_prev) out_prev[d] = key;
+            if (out_id) out_id[d] = __float_as_uint(vel[slot0 + q].w);
+        }
+    }
+}
+
+__global__ void compact_overflow_kernel(const BoxDesc* boxes, int nboxes, uint64_t step, const float4* ov_pos,
+                                        const float4* ov_vel, const DeviceState* st, unsigned parity, uint32_t ov_cap,
+                                        const uint32_t* offsets, uint64_t cells, uint64_t n_total,
+                                        uint64_t total_slots, uint32_t* out_cell, uint32_t* out_slot,
+                                        uint32_t* out_prev, uint32_t* out_id)
+{
+    const uint32_t n = min(st->ov_count[parity], ov_cap);
+    const uint32_t base = offsets[cells];
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const uint64_t d = (uint64_t)base + q;
+        if (d >= n_total) break;
+        if (out_cell) {   // the cell the particle was keyed to (streamed with the shift of step `step`)
+            const float4 p = ov_pos[q], w = ov_vel[q];
+            const int bi = box_of_particle(boxes, nboxes, __float_as_uint(w.w));
+            const BoxDesc& b = boxes[bi];
+            float3 v = make_float3(w.x, w.y, w.z);
+            const float3 xs = stream_shift(b, make_float3(p.x, p.y, p.z), v, grid_shift(b, bi, step, st));
+            out_cell[d] = b.cell_base + ref_index(b, cell_of(b, xs));
+        }
+        if (out_slot) out_slot[d] = (uint32_t)(total_slots + q);
+        if (out_prev) out_prev[d] = __float_as_uint(ov_pos[q].w);
+        if (out_id) out_id[d] = __float_as_uint(ov_vel[q].w);
+    }
+}
+
+// Getter: every stored particle to its id in dense (N, 3) arrays.
+__global__ void __launch_bounds__(kThreads) gather_kernel(const StepArgs a, const uint32_t* count, const float4* pos,
+                                                          const float4* vel, uint64_t cells, uint64_t n_total,
+                                                          const float4* ov_pos,
+                                                          const float4* ov_vel, unsigned parity, float* out_pos,
+                                                          float* out_vel, unsigned int* n_seen)
+{
+    uint32_t seen = 0;
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells;
+         c += (uint64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = a.nboxes - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a.boxes[mid].cell_base <= c) lo = mid; else hi = mid - 1;
+        }
+        const BoxDesc& b = a.boxes[lo];
+        const uint32_t n = min(count[c], b.cap);
+        const uint64_t slot0 = b.slot_base + (c - b.cell_base) * b.cap;
+        for (uint32_t q = 0; q < n; ++q) {
+            const float4 x = pos[slot0 + q], w = vel[slot0 + q];
+            const uint64_t id = __float_as_uint(w.w);
+            if (id >= n_total) {
+                atomicOr(&a.state->error_flags, kErrKeyMismatch);
+                continue;
+            }
+            if (out_pos) { out_pos[3 * id] = x.x; out_pos[3 * id + 1] = x.y; out_pos[3 * id + 2] = x.z; }
+            if (out_vel) { out_vel[3 * id] = w.x; out_vel[3 * id + 1] = w.y; out_vel[3 * id + 2] = w.z; }
+        }
+        seen += n;
+    }
+    if (blockIdx.x == 0) {
+        const uint32_t m = min(a.state->ov_count[parity], a.ov_cap);
+        for (uint32_t q = threadIdx.x; q < m; q += blockDim.x) {
+            const float4 x = ov_pos[q], w = ov_vel[q];
+            const uint64_t id = __float_as_uint(w.w);
+            if (id >= n_total) {
+                atomicOr(&a.state->error_flags, kErrKeyMismatch);
+                continue;
+            }
+            if (out_pos) { out_pos[3 * id] = x.x; out_pos[3 * id + 1] = x.y; out_pos[3 * id + 2] = x.z; }
+            if (out_vel) { out_vel[3 * id] = w.x; out_vel[3 * id + 1] = w.y; out_vel[3 * id + 2] = w.z; }
+        }
+        if (threadIdx.x == 0) seen += m;
+    }
+    atomicAdd(n_seen, seen);
+}
+
+// ------------------------------------------------------------------ initialisation
+
+// Uniform positions in the fluid volume (channel: inside the cylinder of radius
+// (Lz-2)/2 in y-z), Maxwell-Boltzmann velocities (simulation_kernels.cu:22-58).
+__global__ void init_kernel(const BoxDesc* boxes, int nboxes, float* pos, float* vel, uint64_t n_total)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_total;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nboxes - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (boxes[mid].dense_base <= i) lo = mid; else hi = mid - 1;
+        }
+        const BoxDesc& b = boxes[lo];
+        const uint64_t k = i - b.dense_base;
+        float sc[3];
+        for (int d = 0; d < 3; ++d) sc[d] = b.Lf[d] - (float)(2 * (1 - b.periodic[d]));
+        float3 x;
+        uint32_t attempt = 0;
+        while (true) {
+            const uint4 o = philox4x32_10(make_uint4((uint32_t)k, (uint32_t)(k >> 32), kInit, 2 * attempt),
+                                          b.seed_lo, b.seed_hi);
+            x = make_float3((u01(o.x) - 0.5f) * sc[0], (u01(o.y) - 0.5f) * sc[1], (u01(o.z) - 0.5f) * sc[2]);
+            if (!b.channel || (x.z * x.z + x.y * x.y) <= b.R2 || attempt > 64) break;
+            ++attempt;
+        }
+        const uint4 o = philox4x32_10(make_uint4((uint32_t)k, (uint32_t)(k >> 32), kInit, 1u), b.seed_lo, b.seed_hi);
+        float g0, g1, g2, g3;
+        box_muller(o.x, o.y, g0, g1);
+        box_muller(o.z, o.w, g2, g3);
+        pos[3 * i] = x.x; pos[3 * i + 1] = x.y; pos[3 * i + 2] = x.z;
+        vel[3 * i] = g0 * b.tv; vel[3 * i + 1] = g1 * b.tv; vel[3 * i + 2] = g2 * b.tv;
+    }
+}
+
+// Velocity sums of particles [begin, end) in FP64, one partial per block, in a
+// fixed order (the host adds the partials), so momentum removal is deterministic.
+__global__ void momentum_partial_kernel(const float* vel, uint64_t begin, uint64_t end, double* partial)
+{
+    __shared__ double red[3][kThreads];
+    double sx = 0, sy = 0, sz = 0;
+    for (uint64_t i = begin + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < end;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        sx += vel[3 * i]; sy += vel[3 * i + 1]; sz += vel[3 * i + 2];
+    }
+    red[0][threadIdx.x] = sx; red[1][threadIdx.x] = sy; red[2][threadIdx.x] = sz;
+    __syncthreads();
+    for (int o = kThreads / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o)
+            for (int d = 0; d < 3; ++d) red[d][threadIdx.x] += red[d][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int d = 0; d < 3; ++d) partial[3 * blockIdx.x + d] = red[d][0];
+}
+
+__global__ void subtract_kernel(float* vel, uint64_t begin, uint64_t end, float mx, float my, float mz)
+{
+    for (uint64_t i = begin + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < end;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        vel[3 * i] -= mx; vel[3 * i + 1] -= my; vel[3 * i + 2] -= mz;
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+
+size_t step_smem_bytes(uint32_t pbuf) { return (size_t)pbuf * (16 + 16 + 2 + 2 + 2); }
+
+cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st)
+{
+    const size_t smem = step_smem_bytes(pbuf);
+    if (algorithm == 0 && !table) step_kernel<0, false><<<grid, kThreads, smem, st>>>(a, pbuf);
+    else if (algorithm == 0) step_kernel<0, true><<<grid, kThreads, smem, st>>>(a, pbuf);
+    else if (!table) step_kernel<1, false><<<grid, kThreads, smem, st>>>(a, pbuf);
+    else step_kernel<1, true><<<grid, kThreads, smem, st>>>(a, pbuf);
+    return cudaGetLastError();
+}
+
+cudaError_t configure_step(int algorithm, uint32_t pbuf, int* blocks_per_sm)
+{
+    const size_t smem = step_smem_bytes(pbuf);
+    const void* fns[4] = {(const void*)step_kernel<0, false>, (const void*)step_kernel<0, true>,
+                          (const void*)step_kernel<1, false>, (const void*)step_kernel<1, true>};
+    for (const void* f : fns) {
+        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fns[algorithm ? 2 : 0], kThreads, smem);
+}
+
+cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel, uint64_t n_total, int grid,
+                           cudaStream_t st)
+{
+    scatter_kernel<<<grid, kThreads, 0, st>>>(a, pos, vel, n_total);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sample_finalize(float4* samp, SampleAcc* acc, uint64_t cells, int snapshot, int grid,
+                                   cudaStream_t st)
+{
+    sample_finalize_kernel<<<grid, kThreads, 0, st>>>(samp, acc, cells, snapshot);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_layout(const StepArgs& a, const uint32_t* count, const float4* pos, const float4* vel,
+                          uint32_t* offsets, uint64_t cells, uint64_t n_total, unsigned long long* status,
+                          unsigned int* tile_counter, const float4* ov_pos, const float4* ov_vel, unsigned parity,
+                          uint32_t* out_cell, uint32_t* out_slot, uint32_t* out_prev, uint32_t* out_id, int grid,
+                          cudaStream_t st)
+{
+    const uint64_t tiles = (cells + kThreads * kScanItems - 1) / (kThreads * kScanItems);
+    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(unsigned long long) * tiles, st);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(tile_counter, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return e;
+    scan_kernel<<<(unsigned)tiles, kThreads, 0, st>>>(count, a.boxes, a.nboxes, cells, offsets, status, tile_counter,
+                                                      a.state);
+    compact_kernel<<<grid, kThreads, 0, st>>>(a, count, pos, vel, offsets, cells, n_total, out_cell, out_slot,
+                                              out_prev, out_id);
+    compact_overflow_kernel<<<8, kThreads, 0, st>>>(a.boxes, a.nboxes, a.step, ov_pos, ov_vel, a.state, parity,
+                                                    a.ov_cap, offsets, cells, n_total, a.total_slots, out_cell,
+                                                    out_slot, out_prev, out_id);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const StepArgs& a, const uint32_t* count, const float4* pos, const float4* vel,
+                          uint64_t cells, uint64_t n_total, const float4* ov_pos, const float4* ov_vel, unsigned parity,
+                          float* out_pos, float* out_vel, unsigned int* n_seen, int grid, cudaStream_t st)
+{
+    gather_kernel<<<grid, kThreads, 0, st>>>(a, count, pos, vel, cells, n_total, ov_pos, ov_vel, parity, out_pos,
+                                             out_vel, n_seen);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init(const BoxDesc* boxes, int nboxes, float* pos, float* vel, uint64_t n_total, int grid,
+                        cudaStream_t st)
+{
+    init_kernel<<<grid, kThreads, 0, st>>>(boxes, nboxes, pos, vel, n_total);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_momentum_partial(const float* vel, uint64_t begin, uint64_t end, double* partial, int grid,
+                                    cudaStream_t st)
+{
+    momentum_partial_kernel<<<grid, kThreads, 0, st>>>(vel, begin, end, partial);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_subtract(float* vel, uint64_t begin, uint64_t end, float mx, float my, float mz, int grid,
+                            cudaStream_t st)
+{
+    subtract_kernel<<<grid, kThreads, 0, st>>>(vel, begin, end, mx, my, mz);
+    return cudaGetLastError();
+}
+
+size_t scan_status_words(uint64_t cells) { return (cells + kThreads * kScanItems - 1) / (kThreads * kScanItems); }
+
+}  // namespace mpcd_gb

@@ -1,0 +1,45 @@
+// Launchers of the GB300 MPCD kernels (host side).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mpcd_types.h"
+
+namespace mpcd_gb {
+
+// Dynamic shared memory of the step kernel for a particle buffer of `pbuf` entries.
+size_t step_smem_bytes(uint32_t pbuf);
+// Opt the step kernels into `pbuf` and report resident CTAs per SM.
+cudaError_t configure_step(int algorithm, uint32_t pbuf, int* blocks_per_sm);
+// One step of every box (algorithm 0 = SRD, 1 = extended; table = injected draws).
+cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st);
+// Key dense clean particles for step a.step + 1 and scatter them into a.out_*.
+cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel, uint64_t n_total, int grid,
+                           cudaStream_t st);
+// Lab-grid sample of one step into the FP64 running sums (and clear the step sums).
+cudaError_t launch_sample_finalize(float4* samp, SampleAcc* acc, uint64_t cells, int snapshot, int grid,
+                                   cudaStream_t st);
+// Layout dump: cells in storage order, stable order within a cell (decoupled
+// look-back scan of the counts, then one thread per cell), then the overflow
+// list.  offsets: cells + 1 entries.
+cudaError_t launch_layout(const StepArgs& a, const uint32_t* count, const float4* pos, const float4* vel,
+                          uint32_t* offsets, uint64_t cells, uint64_t n_total, unsigned long long* status,
+                          unsigned int* tile_counter, const float4* ov_pos, const float4* ov_vel, unsigned parity,
+                          uint32_t* out_cell, uint32_t* out_slot, uint32_t* out_prev, uint32_t* out_id, int grid,
+                          cudaStream_t st);
+// Getter: every stored particle to its id in (N, 3) arrays; n_seen += particles written.
+cudaError_t launch_gather(const StepArgs& a, const uint32_t* count, const float4* pos, const float4* vel,
+                          uint64_t cells, uint64_t n_total, const float4* ov_pos, const float4* ov_vel, unsigned parity,
+                          float* out_pos, float* out_vel, unsigned int* n_seen, int grid, cudaStream_t st);
+size_t scan_status_words(uint64_t cells);
+// Initial particles (uniform positions, Maxwell-Boltzmann velocities).
+cudaError_t launch_init(const BoxDesc* boxes, int nboxes, float* pos, float* vel, uint64_t n_total, int grid,
+                        cudaStream_t st);
+cudaError_t launch_momentum_partial(const float* vel, uint64_t begin, uint64_t end, double* partial, int grid,
+                                    cudaStream_t st);
+cudaError_t launch_subtract(float* vel, uint64_t begin, uint64_t end, float mx, float my, float mz, int grid,
+                            cudaStream_t st);
+
+}  // namespace mpcd_gb

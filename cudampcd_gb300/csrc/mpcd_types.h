@@ -1,0 +1,106 @@
+// Host/device data structures of the GB300 MPCD step.
+//
+// Particles live in per-cell buckets: cell c of a box owns `cap` slots
+// (cap = 4n, the depth of the reference's cell table, backend_context.cu:24),
+// stored as two float4 arrays: pos = (x, y, z, prev) and vel = (vx, vy, vz, 0),
+// where `prev` is the particle's position in the previous layout (its stable
+// sort key).  Cells are numbered in storage order, z fastest, then x, then y,
+// so that the up to 27 source cells of any destination cell are processed
+// within a short window of the sweep.  Two bucket sets alternate by step parity.
+#pragma once
+
+#include <cstdint>
+
+namespace mpcd_gb {
+
+constexpr int kThreads = 256;        // threads per CTA of the step kernel
+constexpr int kMaxTileCells = 128;   // cells per tile, upper bound
+constexpr int kMaxInjectedShifts = 4;
+
+// One simulation box (a "replica" in a batched ensemble).
+struct BoxDesc {
+    int32_t L[3];          // container size incl. wall layers
+    float Lf[3];
+    int32_t periodic[3];
+    int32_t wall_z;        // periodicity.z == 0: bounce-back walls and ghost layers in z
+    int32_t channel;       // ExperimentType::channel
+    float dt;
+    float drag_dt;         // drag * dt, added to v.x after a collision
+    float tv;              // thermal velocity sqrt(T)
+    float R2;              // channel radius^2, (Lz - 2)^2 / 4
+    float cos_a, sin_a;    // SRD rotation by 120 degrees (host libm, as the reference)
+    uint32_t n;            // particles per cell
+    uint32_t cap;          // bucket depth, 4n
+    uint32_t C;            // cells
+    uint32_t N;            // particles
+    uint32_t cell_base;    // first global cell of this box
+    uint32_t tile_base;    // first tile of this box
+    uint32_t tiles;        // tiles of this box
+    uint32_t tile_cells;   // cells per tile
+    uint64_t slot_base;    // first global slot of this box
+    uint64_t dense_base;   // first particle of this box in dense (getter) arrays
+    uint32_t seed_lo, seed_hi;
+};
+
+// FP64 running sums of the lab-grid sample of one cell.
+struct alignas(32) SampleAcc {
+    double n, vx, vy, vz;
+};
+
+// Device-resident bookkeeping shared by all launches of a handle.
+struct DeviceState {
+    unsigned long long overflow_total;   // particles that found their bucket full
+    unsigned int error_flags;            // kErr* bits
+    unsigned int ov_count[2];            // overflow list fill, by step parity
+    unsigned int pad;
+    // injected grid shifts (test hook), valid when inject_valid[i] != 0
+    unsigned long long inject_step[kMaxInjectedShifts];
+    float inject_shift[kMaxInjectedShifts][4];
+    unsigned int inject_valid[kMaxInjectedShifts];
+};
+
+enum : unsigned int {
+    kErrOverflowListFull = 1u,
+    kErrWaitTimeout = 2u,
+    kErrKeyMismatch = 4u,
+};
+
+// Injected per-cell draws (reference cell order of box 0), test hook.
+struct DrawTables {
+    const uint32_t* ghost_count;
+    const float* ghost_pos;
+    const float* ghost_vel;
+    const float* axis;
+    const float* gate_u;
+    const float* gauss;
+    uint32_t gmax, pmax;
+};
+
+struct StepArgs {
+    const BoxDesc* boxes;
+    int32_t nboxes;
+    uint32_t num_tiles;
+    uint64_t total_slots;
+    uint64_t step;                // k: this launch completes step k
+    // buckets holding clean(k), keyed by the cell after streaming step k
+    const float4* in_pos;
+    const float4* in_vel;
+    uint32_t* in_count;           // zeroed as read
+    // buckets receiving clean(k+1), keyed by the cell after streaming step k+1
+    float4* out_pos;
+    float4* out_vel;
+    uint32_t* out_count;
+    // overflow lists: in = pending for step k, out = for step k+1
+    const float4* ov_in_pos;
+    const float4* ov_in_vel;
+    float4* ov_out_pos;
+    float4* ov_out_vel;
+    uint32_t ov_cap;
+    DeviceState* state;
+    int32_t sample;               // accumulate the lab-grid sample of clean(k+1)
+    float4* samp;                 // [global cells] (sum vx, vy, vz, count)
+    float ext_axis[13][3];        // discrete axis set of the extended collision
+    DrawTables draws;             // used by the injected-draw instantiation
+};
+
+}  // namespace mpcd_gb

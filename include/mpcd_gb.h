@@ -1,0 +1,157 @@
+/*
+ * mpcd_gb.h -- C ABI of the GB300 MPCD time step (libmpcd_gb.so).
+ *
+ * This is the drop-in boundary for the MPCD step of azantop/cudaMPCD.  The
+ * reference reaches its CUDA path through the abstract C++ class
+ * mpcd::Backend (src/libmpcd/common/backend.hpp:11-31), created by
+ * mpcd::create_backend(params, "cuda") (src/libmpcd/common/backend_factory.hpp:15-27)
+ * for mpcd::api::SimulationHandle (src/libmpcd/api/simulator_handle.cpp:9).
+ * Every Backend member maps onto one function below; a Backend subclass that
+ * forwards to them is all the reference tree needs.
+ *
+ * Conventions
+ *   - plain pointers and sizes; host buffers unless a name says "device";
+ *   - every function returns 0 on success and a negative MPCD_GB_E* code on
+ *     failure; mpcd_gb_last_error() then describes the failure (the reference
+ *     throws std::runtime_error, src/libmpcd/cuda_backend/gpu_error_check.hpp:10-39);
+ *   - a handle owns one CUDA stream and all device memory of one simulation;
+ *     calls on one handle must not overlap (the reference is single-threaded);
+ *   - positions and velocities are (N, 3) float32, xyz interleaved, indexed
+ *     by particle id: the order fixed when the handle is created, unchanged by
+ *     steps (the reference returns its internal array order, which its CUDA
+ *     backend permutes every 100 steps, cuda_backend_impl.cu:127-128).
+ */
+#ifndef MPCD_GB_H
+#define MPCD_GB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPCD_GB_ABI_VERSION 1
+
+enum {
+    MPCD_GB_OK = 0,
+    MPCD_GB_EINVAL = -1,    /* bad argument or parameter */
+    MPCD_GB_ECUDA = -2,     /* CUDA runtime error */
+    MPCD_GB_ENOMEM = -3,    /* device allocation failed */
+    MPCD_GB_EDEVICE = -4,   /* device-side check failed (overflow list full, wait timeout, ...) */
+    MPCD_GB_ESTATE = -5     /* call not valid in the current state */
+};
+
+/* Mirrors mpcd::SimulationParameters (include/mpcd/api/simulation_parameters.hpp:70-102)
+ * for the fields the step reads, plus a Philox seed (the reference seeds from
+ * /dev/urandom and has no seed field). */
+typedef struct mpcd_gb_params {
+    int32_t experiment;        /* 0 standard, 1 channel (ExperimentType) */
+    int32_t algorithm;         /* 0 srd, 1 extended (MPCDAlgorithm) */
+    int32_t collision_kernel;  /* accepted for compatibility (CollisionKernel); one fused kernel serves all */
+    int32_t periodicity[3];
+    float volume_size[3];      /* container size incl. wall layers, integral */
+    uint32_t N;                /* ignored: N = n * fluid volume (see mpcd_gb_num_particles) */
+    uint32_t n;                /* particles per cell */
+    uint32_t device_id;
+    float delta_t;
+    float temperature;
+    float thermal_velocity;
+    float drag;
+    uint64_t seed;             /* Philox key */
+} mpcd_gb_params;
+
+typedef struct mpcd_gb_handle mpcd_gb_handle;
+
+/* ABI version of the loaded library (== MPCD_GB_ABI_VERSION). */
+int32_t mpcd_gb_abi_version(void);
+
+/* Replaces CudaBackend::CudaBackend (src/libmpcd/cuda_backend/cuda_backend.cu:7) /
+ * BackendContext::BackendContext (src/libmpcd/cuda_backend/backend_context.cu:17-127):
+ * allocate, distribute particles uniformly in the fluid volume with
+ * Maxwell-Boltzmann velocities (net momentum removed). */
+int32_t mpcd_gb_create(const mpcd_gb_params *params, mpcd_gb_handle **out);
+
+/* Replaces CudaBackend::~CudaBackend (src/libmpcd/cuda_backend/cuda_backend_impl.cu:20-22). */
+void mpcd_gb_destroy(mpcd_gb_handle *h);
+
+/* Failure description of the last call on h (h may be NULL for mpcd_gb_create failures). */
+const char *mpcd_gb_last_error(const mpcd_gb_handle *h);
+
+/* Replaces Backend::step (backend.hpp:15; cuda_backend_impl.cu:111-131). */
+int32_t mpcd_gb_step(mpcd_gb_handle *h, int32_t n_steps);
+
+/* Replaces Backend::stepAndAccumulateSample (backend.hpp:17; cuda_backend_impl.cu:182-204). */
+int32_t mpcd_gb_step_and_sample(mpcd_gb_handle *h, int32_t n_steps);
+
+/* Replaces Backend::getSampleMean (backend.hpp:18; cuda_backend_impl.cu:206-218).
+ * density: C floats, velocity: 3C floats (xyz interleaved), cell order x + Lx*(y + Ly*z).
+ * Divides by the sample counter, S-1 for S sampled steps, as the reference does. */
+int32_t mpcd_gb_get_sample_mean(mpcd_gb_handle *h, float *density, float *velocity);
+
+/* Replaces Backend::getNParticles (backend.hpp:20). */
+size_t mpcd_gb_num_particles(const mpcd_gb_handle *h);
+
+/* Number of cells C = Lx*Ly*Lz (container). */
+size_t mpcd_gb_num_cells(const mpcd_gb_handle *h);
+
+/* Replace Backend::getParticlePositions / getParticleVelocities (backend.hpp:21-22). out: 3N floats. */
+int32_t mpcd_gb_get_positions(mpcd_gb_handle *h, float *out);
+int32_t mpcd_gb_get_velocities(mpcd_gb_handle *h, float *out);
+
+/* Replace Backend::setParticlePositions / setParticleVelocities / setParticles (backend.hpp:23-25).
+ * in: 3N floats indexed by particle id.  (The reference's CUDA setters index
+ * the particle array with the float index, cuda_backend_impl.cu:157-180.) */
+int32_t mpcd_gb_set_positions(mpcd_gb_handle *h, const float *in);
+int32_t mpcd_gb_set_velocities(mpcd_gb_handle *h, const float *in);
+int32_t mpcd_gb_set_particles(mpcd_gb_handle *h, const float *positions, const float *velocities);
+
+/* ---- stream and timing (used by bench.py; no reference counterpart) ---- */
+
+/* Run the handle's work on an existing stream (cudaStream_t passed as void*); NULL = own stream. */
+int32_t mpcd_gb_set_stream(mpcd_gb_handle *h, void *stream);
+/* Block until the handle's stream is idle. */
+int32_t mpcd_gb_synchronize(mpcd_gb_handle *h);
+/* Run n_steps steps between two CUDA events recorded on the handle's stream; returns
+ * the elapsed device time and the elapsed time of the step kernel launches alone. */
+int32_t mpcd_gb_time_steps(mpcd_gb_handle *h, int32_t n_steps, float *total_ms, float *kernel_ms);
+
+/* ---- test hooks (no reference counterpart; used by the parity tests) ---- */
+
+/* Current step index (the Philox step counter). */
+uint64_t mpcd_gb_step_index(const mpcd_gb_handle *h);
+
+/* Use `shift` as the grid shift of step `step` instead of the Philox draw
+ * (the reference draws it on the host, cuda_backend_impl.cu:85-87).  Up to 4 pending. */
+int32_t mpcd_gb_inject_shift(mpcd_gb_handle *h, uint64_t step, const float shift[3]);
+
+/* The grid shift the handle uses for `step`. */
+int32_t mpcd_gb_get_shift(mpcd_gb_handle *h, uint64_t step, float shift[3]);
+
+/* Layout of the current cell buckets -- the counting sort by cell -- one entry
+ * per particle in layout order (cells in storage order z fastest, then x, then
+ * y; stable order within a cell; then particles waiting in the overflow list):
+ * cell = reference cell index x + Lx*(y + Ly*z) of the bucket, slot = sparse
+ * slot id, prev = position in the previous layout (slot id, or the index into
+ * the arrays given to a setter), id = particle id.  counts: C entries
+ * (reference cell order), the number of particles each cell received, overflow
+ * included (the reference's uniform_counter).  Any pointer may be NULL. */
+int32_t mpcd_gb_dump_layout(mpcd_gb_handle *h, uint32_t *cell, uint32_t *slot, uint32_t *prev, uint32_t *id,
+                            uint32_t *counts);
+
+/* Injected draws for the next step (the oracle's recorded tables, reference
+ * cell order): ghost_count[C], ghost_pos[C*gmax*3], ghost_vel[C*gmax*3],
+ * axis[C*3], gate_u[C], gauss[C*pmax].  The next mpcd_gb_step consumes them;
+ * pass NULL tables to return to Philox draws. */
+int32_t mpcd_gb_inject_draws(mpcd_gb_handle *h, uint32_t gmax, uint32_t pmax, const uint32_t *ghost_count,
+                             const float *ghost_pos, const float *ghost_vel, const float *axis,
+                             const float *gate_u, const float *gauss);
+
+/* Device-side counters: [0] particles that overflowed a cell bucket (all time),
+ * [1] error flags (bit 0 overflow list full, bit 1 wait timeout, bit 2 key mismatch). */
+int32_t mpcd_gb_counters(mpcd_gb_handle *h, uint64_t out[2]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

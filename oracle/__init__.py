@@ -118,6 +118,13 @@ def lib():
         L.orc_stable_perm.argtypes = [u32p, C.c_size_t, C.c_uint32, u32p]
         L.orc_time_reference_steps.argtypes = [C.POINTER(OrcParams), C.c_uint64, C.c_int32]
         L.orc_time_reference_steps.restype = C.c_double
+        L.orc_run_create.argtypes = [C.POINTER(OrcParams), C.c_uint64]
+        L.orc_run_create.restype = C.c_void_p
+        L.orc_run_steps.argtypes = [C.c_void_p, C.c_int32]
+        L.orc_run_steps.restype = C.c_int
+        L.orc_run_particles.argtypes = [C.c_void_p]
+        L.orc_run_particles.restype = C.c_size_t
+        L.orc_run_destroy.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -339,3 +346,26 @@ def reference_steps(box: Box, pos, vel, rng: OrcXoshiro, nsteps: int, sampler: S
 def time_reference_steps(box: Box, seed: int, steps: int) -> float:
     p = box.cstruct()
     return float(lib().orc_time_reference_steps(C.byref(p), seed, steps))
+
+
+class Run:
+    """A box advanced by the restated reference CPU step (used for the CPU baseline)."""
+
+    def __init__(self, box: Box, seed: int):
+        self._p = box.cstruct()
+        self._h = lib().orc_run_create(C.byref(self._p), seed)
+        if not self._h:
+            raise MemoryError("oracle run allocation failed")
+        self.N = int(lib().orc_run_particles(self._h))
+
+    def steps(self, n: int) -> None:
+        if lib().orc_run_steps(self._h, n):
+            raise RuntimeError("oracle step failed")
+
+    def close(self) -> None:
+        if self._h:
+            lib().orc_run_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

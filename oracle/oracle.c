@@ -914,3 +914,47 @@ double orc_time_reference_steps(const orc_params *p, uint64_t seed, int32_t step
     free(pos); free(vel); free(cell); free(counter); free(table);
     return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
 }
+
+struct orc_run {
+    orc_params p;
+    size_t N, C;
+    float *pos, *vel;
+    uint32_t *cell, *counter, *table;
+    orc_xoshiro rng;
+};
+
+orc_run *orc_run_create(const orc_params *p, uint64_t seed)
+{
+    orc_run *r = (orc_run *)calloc(1, sizeof(orc_run));
+    if (!r) return NULL;
+    r->p = *p;
+    r->C = (size_t)p->L[0] * p->L[1] * p->L[2];
+    r->N = p->n_density;
+    for (int a = 0; a < 3; ++a) r->N *= (size_t)(p->L[a] - 2 * (1 - p->periodic[a]));
+    r->pos = (float *)malloc(sizeof(float) * 3 * r->N);
+    r->vel = (float *)malloc(sizeof(float) * 3 * r->N);
+    r->cell = (uint32_t *)malloc(sizeof(uint32_t) * r->N);
+    r->counter = (uint32_t *)malloc(sizeof(uint32_t) * r->C);
+    r->table = (uint32_t *)malloc(sizeof(uint32_t) * r->C * p->cap);
+    if (!r->pos || !r->vel || !r->cell || !r->counter || !r->table) {
+        orc_run_destroy(r);
+        return NULL;
+    }
+    orc_xoshiro_seed(&r->rng, seed, seed ^ 0x9E3779B97F4A7C15ull);
+    orc_distribute(p, r->pos, r->vel, r->cell, r->N, &r->rng);
+    return r;
+}
+
+int orc_run_steps(orc_run *r, int32_t n)
+{
+    return orc_reference_steps(&r->p, r->pos, r->vel, r->cell, r->N, &r->rng, n, r->counter, r->table, NULL);
+}
+
+size_t orc_run_particles(const orc_run *r) { return r->N; }
+
+void orc_run_destroy(orc_run *r)
+{
+    if (!r) return;
+    free(r->pos); free(r->vel); free(r->cell); free(r->counter); free(r->table);
+    free(r);
+}

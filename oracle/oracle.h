@@ -155,6 +155,13 @@ void orc_stable_perm(const uint32_t *key, size_t N, uint32_t nkeys, uint32_t *pe
  * freshly distributed box; returns elapsed seconds of the stepping loop. */
 double orc_time_reference_steps(const orc_params *p, uint64_t seed, int32_t steps);
 
+/* A persistent box advanced by the restated reference step (CPU baseline). */
+typedef struct orc_run orc_run;
+orc_run *orc_run_create(const orc_params *p, uint64_t seed);
+int orc_run_steps(orc_run *r, int32_t n);
+size_t orc_run_particles(const orc_run *r);
+void orc_run_destroy(orc_run *r);
+
 #ifdef __cplusplus
 }
 #endif
