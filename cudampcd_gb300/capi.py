@@ -67,7 +67,7 @@ def lib() -> C.CDLL:
         L.mpcd_gb_step_index.restype = C.c_uint64
         L.mpcd_gb_inject_shift.argtypes = [H, C.c_uint64, f32p]
         L.mpcd_gb_get_shift.argtypes = [H, C.c_uint64, f32p]
-        L.mpcd_gb_dump_layout.argtypes = [H, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.mpcd_gb_dump_layout.argtypes = [H, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.mpcd_gb_inject_draws.argtypes = [H, C.c_uint32, C.c_uint32] + [C.c_void_p] * 6
         L.mpcd_gb_counters.argtypes = [H, u64p]
         _lib = L
@@ -160,15 +160,14 @@ class Handle:
         return out
 
     def layout(self):
-        """(cell, slot, prev, id, counts) of the current bucket layout (see mpcd_gb_dump_layout)."""
+        """(cell, slot, id, counts) of the current bucket layout (see mpcd_gb_dump_layout)."""
         cell = np.zeros(self.N, np.uint32)
         slot = np.zeros(self.N, np.uint32)
-        prev = np.zeros(self.N, np.uint32)
         pid = np.zeros(self.N, np.uint32)
         counts = np.zeros(self.C, np.uint32)
-        self._check(self._lib.mpcd_gb_dump_layout(self.h, cell.ctypes.data, slot.ctypes.data, prev.ctypes.data,
-                                                  pid.ctypes.data, counts.ctypes.data))
-        return cell, slot, prev, pid, counts
+        self._check(self._lib.mpcd_gb_dump_layout(self.h, cell.ctypes.data, slot.ctypes.data, pid.ctypes.data,
+                                                  counts.ctypes.data))
+        return cell, slot, pid, counts
 
     def inject_draws(self, draws):
         """draws: oracle.Draws tables (reference cell order); None returns to Philox draws."""

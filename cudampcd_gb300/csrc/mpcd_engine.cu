@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -186,20 +187,22 @@ public:
         check_device_errors();
     }
 
-    void dump(uint32_t* cell, uint32_t* slot, uint32_t* prev, uint32_t* id, uint32_t* counts)
+    void dump(uint32_t* cell, uint32_t* slot, uint32_t* id, uint32_t* counts)
     {
-        DeviceBuffer dc, ds, dp, di;
+        DeviceBuffer dc, ds, di;
         check(dc.alloc(sizeof(uint32_t) * N_), "dump alloc");
         check(ds.alloc(sizeof(uint32_t) * N_), "dump alloc");
-        check(dp.alloc(sizeof(uint32_t) * N_), "dump alloc");
         check(di.alloc(sizeof(uint32_t) * N_), "dump alloc");
-        layout(dc.as<uint32_t>(), ds.as<uint32_t>(), dp.as<uint32_t>(), di.as<uint32_t>());
-        if (cell) check(cudaMemcpyAsync(cell, dc.p, sizeof(uint32_t) * N_, cudaMemcpyDeviceToHost, stream_), "dump");
-        if (slot) check(cudaMemcpyAsync(slot, ds.p, sizeof(uint32_t) * N_, cudaMemcpyDeviceToHost, stream_), "dump");
-        if (prev) check(cudaMemcpyAsync(prev, dp.p, sizeof(uint32_t) * N_, cudaMemcpyDeviceToHost, stream_), "dump");
-        if (id) check(cudaMemcpyAsync(id, di.p, sizeof(uint32_t) * N_, cudaMemcpyDeviceToHost, stream_), "dump");
+        layout(dc.as<uint32_t>(), ds.as<uint32_t>(), nullptr, di.as<uint32_t>());
+        std::vector<uint32_t> hc(N_), hs(N_), hi(N_);
+        check(cudaMemcpyAsync(hc.data(), dc.p, sizeof(uint32_t) * N_, cudaMemcpyDeviceToHost, stream_), "dump");
+        check(cudaMemcpyAsync(hs.data(), ds.p, sizeof(uint32_t) * N_, cudaMemcpyDeviceToHost, stream_), "dump");
+        check(cudaMemcpyAsync(hi.data(), di.p, sizeof(uint32_t) * N_, cudaMemcpyDeviceToHost, stream_), "dump");
         check(cudaStreamSynchronize(stream_), "dump");
-        sort_overflow_tail(cell, slot, prev, id);
+        sort_overflow_tail(hc.data(), hs.data(), hi.data());
+        if (cell) std::copy(hc.begin(), hc.end(), cell);
+        if (slot) std::copy(hs.begin(), hs.end(), slot);
+        if (id) std::copy(hi.begin(), hi.end(), id);
         if (counts) {
             std::vector<uint32_t> raw(cells_);
             check(cudaMemcpyAsync(raw.data(), count_[parity()].p, sizeof(uint32_t) * cells_, cudaMemcpyDeviceToHost,
@@ -217,19 +220,19 @@ public:
     }
 
     // The overflow list is filled in arrival order; order its part of a dump by
-    // (cell, prev) so that a dump is deterministic.
-    void sort_overflow_tail(uint32_t* cell, uint32_t* slot, uint32_t* prev, uint32_t* id)
+    // (cell, id) so that a dump is deterministic.
+    void sort_overflow_tail(uint32_t* cell, uint32_t* slot, uint32_t* id)
     {
         DeviceState st;
         check(cudaMemcpy(&st, state_.p, sizeof st, cudaMemcpyDeviceToHost), "dump");
         const uint64_t m = std::min(st.ov_count[parity()], ov_cap_);
-        if (m < 2 || !cell || !prev) return;
+        if (m < 2) return;
         const uint64_t base = N_ - m;
         std::vector<uint64_t> order(m);
         for (uint64_t i = 0; i < m; ++i) order[i] = i;
         std::sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) {
             const uint32_t ca = cell[base + a], cb = cell[base + b];
-            return ca != cb ? ca < cb : prev[base + a] < prev[base + b];
+            return ca != cb ? ca < cb : id[base + a] < id[base + b];
         });
         auto permute = [&](uint32_t* v) {
             if (!v) return;
@@ -239,7 +242,6 @@ public:
         };
         permute(cell);
         permute(slot);
-        permute(prev);
         permute(id);
     }
 
@@ -399,11 +401,23 @@ private:
         b.dense_base = 0;
         b.seed_lo = (uint32_t)p.seed;
         b.seed_hi = (uint32_t)(p.seed >> 32);
+        // tile: a power-of-two number of cells (a group of 256 / cells threads per
+        // cell), about 1300 particles; the buffer holds one cell with all its
+        // ghosts (cap + n = 5n) at least
         pbuf_ = 1536;
         if (5 * b.n > pbuf_) pbuf_ = 5 * b.n;
-        if (pbuf_ > 5000) throw Error(MPCD_GB_EINVAL, "n too large for one cell in shared memory");
-        uint32_t tc = (uint32_t)(pbuf_ / (1.2 * b.n));
-        tc = tc < 1 ? 1 : (tc > (uint32_t)kMaxTileCells ? (uint32_t)kMaxTileCells : tc);
+        if (pbuf_ > 2048) throw Error(MPCD_GB_EINVAL, "n above 409: one cell and its ghosts must fit a tile");
+        uint32_t tc = 128;
+        while (tc > 8 && tc * b.n * 1.15 > pbuf_) tc >>= 1;
+        // tuning overrides (used by the autotuner and the tuning sweeps)
+        if (const char* e = std::getenv("MPCD_GB_PBUF")) {
+            const uint32_t v = (uint32_t)std::strtoul(e, nullptr, 10);
+            if (v >= 5 * b.n && v <= 2048) pbuf_ = v;
+        }
+        if (const char* e = std::getenv("MPCD_GB_TILE_CELLS")) {
+            const uint32_t v = (uint32_t)std::strtoul(e, nullptr, 10);
+            if (v >= 1 && v <= 256 && (v & (v - 1)) == 0) tc = v;
+        }
         b.tile_cells = tc;
         b.tile_base = 0;
         b.tiles = (b.C + tc - 1) / tc;
@@ -462,7 +476,7 @@ private:
     void configure()
     {
         int per_sm = 0;
-        check(configure_step(params_.algorithm, pbuf_, &per_sm), "configure step kernel");
+        check(configure_step(params_.algorithm, pbuf_, boxes_[0].tile_cells, &per_sm), "configure step kernel");
         if (per_sm < 1) throw Error(MPCD_GB_ECUDA, "step kernel does not fit on an SM");
         grid_ = (int)std::min<uint64_t>(tiles_, (uint64_t)sms_ * per_sm);
     }
@@ -494,8 +508,10 @@ private:
     StepArgs args() const
     {
         StepArgs a{};
+        a.box0 = boxes_[0];
         a.boxes = boxes_d_.as<BoxDesc>();
         a.nboxes = (int)boxes_.size();
+        a.boxes_tile_cells = boxes_[0].tile_cells;
         a.num_tiles = (uint32_t)tiles_;
         a.total_slots = total_slots_;
         a.step = step_;
@@ -792,10 +808,9 @@ int32_t mpcd_gb_get_shift(mpcd_gb_handle* h, uint64_t step, float shift[3])
     return guarded(h, [&](mpcd_gb::Engine& e) { e.get_shift(step, shift); });
 }
 
-int32_t mpcd_gb_dump_layout(mpcd_gb_handle* h, uint32_t* cell, uint32_t* slot, uint32_t* prev, uint32_t* id,
-                            uint32_t* counts)
+int32_t mpcd_gb_dump_layout(mpcd_gb_handle* h, uint32_t* cell, uint32_t* slot, uint32_t* id, uint32_t* counts)
 {
-    return guarded(h, [&](mpcd_gb::Engine& e) { e.dump(cell, slot, prev, id, counts); });
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.dump(cell, slot, id, counts); });
 }
 
 int32_t mpcd_gb_inject_draws(mpcd_gb_handle* h, uint32_t gmax, uint32_t pmax, const uint32_t* ghost_count,

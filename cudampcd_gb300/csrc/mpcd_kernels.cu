@@ -182,7 +182,7 @@ __device__ __forceinline__ void sample_add(float4* samp, uint64_t lab, float3 v,
 
 // Write one post-collision particle into its next bucket, or into the overflow list.
 __device__ __forceinline__ void scatter_particle(const StepArgs& a, const BoxDesc& b, float3 x, float3 v,
-                                                 uint32_t prev, uint32_t id, float3 next_shift, bool active)
+                                                 uint32_t id, float3 next_shift, bool active)
 {
     uint64_t key = 0;
     if (active) {
@@ -194,14 +194,14 @@ __device__ __forceinline__ void scatter_particle(const StepArgs& a, const BoxDes
     if (!active) return;
     if (slot < b.cap) {
         const uint64_t at = b.slot_base + (key - b.cell_base) * (uint64_t)b.cap + slot;
-        a.out_pos[at] = make_float4(x.x, x.y, x.z, __uint_as_float(prev));
+        a.out_pos[at] = make_float4(x.x, x.y, x.z, 0.0f);
         a.out_vel[at] = make_float4(v.x, v.y, v.z, __uint_as_float(id));
     } else {
         atomicAdd(&a.state->overflow_total, 1ull);
         const unsigned parity = (unsigned)((a.step + 1) & 1);
         const unsigned q = atomicAdd(&a.state->ov_count[parity], 1u);
         if (q < a.ov_cap) {
-            a.ov_out_pos[q] = make_float4(x.x, x.y, x.z, __uint_as_float(prev));
+            a.ov_out_pos[q] = make_float4(x.x, x.y, x.z, 0.0f);
             a.ov_out_vel[q] = make_float4(v.x, v.y, v.z, __uint_as_float(id));
         } else {
             atomicOr(&a.state->error_flags, kErrOverflowListFull);
@@ -327,30 +327,95 @@ __device__ __forceinline__ void sym_inverse(const float m[6], float tol, float o
 }
 
 // ------------------------------------------------------------------ step kernel
+//
+// One CTA processes tiles of consecutive cells (storage order).  Per tile:
+//   counts (prefetched one tile ahead) and ghost counts, a group of G threads
+//   per cell (G = kThreads / tile cells);
+//   bulk (TMA) copies of every cell's bucket into shared memory + ghosts;
+//   stream step k (recomputed, bit-identical to the scatter that keyed it);
+//   per-cell collision quantities, one group per cell;
+//   per particle: finish the collision, unshift, drag, sample, stream step
+//   k+1 to find the next cell; claim bucket slots with warp-aggregated atomics
+//   (all issued before any result is used) and write the particles out.
+// Order within a cell is canonical: ascending particle id, i.e. the stable sort
+// of the id-ordered particle array by cell.  SRD cell sums are exact 64-bit
+// fixed-point sums (independent of summation order, hence deterministic and
+// splittable over a group); the extended collision walks each cell in id
+// order, as the reference walks it in index order.
 
-struct TileShared {
-    uint32_t cnt[kMaxTileCells];       // real particles staged per cell
-    uint32_t ng[kMaxTileCells];        // ghosts per cell
-    uint32_t off[kMaxTileCells + 1];   // particle offset (real + ghosts) per cell, tile-relative
-    uint32_t goff[kMaxTileCells + 1];  // ghost offset per cell
-    float4 c0[kMaxTileCells];          // SRD: mean, n in w | EXT: mean
-    float4 c1[kMaxTileCells];          // SRD: axis        | EXT: centre of mass
-    float4 c2[kMaxTileCells];          // EXT: omega, participants in w
-    uint32_t warp_tot[kThreads / 32 + 1];
-    uint32_t ov_n;
-    uint32_t abort;
-    uint64_t bar;
+constexpr uint32_t kNoKey = 0xFFFFFFFFu;
+constexpr int kMaxPerThread = 8;   // particle buffer <= kMaxPerThread * kThreads
+
+// Shared memory of one CTA, carved from the dynamic allocation:
+//   particles: pos, vel (float4), next key (u32), cell (u16)
+//   extended only: rank (u16), stable index (u16)
+//   cells: cnt, ng, off, goff (u32, T + 1 each), c0, c1 (float4, T each)
+//   extended only: omega (float4, T)
+struct TileLayout {
+    float4* pos;
+    float4* vel;
+    uint32_t* key;
+    uint16_t* cell;
+    uint16_t* rank;
+    uint16_t* inv;
+    uint32_t *cnt, *ng, *off, *goff;
+    float4 *c0, *c1, *omega;
 };
 
+__host__ __device__ inline size_t tile_smem_bytes(uint32_t pbuf, uint32_t cells, int algorithm)
+{
+    const size_t per_particle = 16 + 16 + 4 + 2 + (algorithm ? 4 : 0);
+    size_t bytes = (size_t)pbuf * per_particle;
+    bytes = (bytes + 15) / 16 * 16 + 4 * (size_t)(cells + 1) * 4;
+    bytes = (bytes + 15) / 16 * 16 + (size_t)cells * 16 * (algorithm ? 3 : 2);
+    return bytes;
+}
+
+__device__ inline TileLayout carve(unsigned char* base, uint32_t pbuf, uint32_t cells, int algorithm)
+{
+    TileLayout t;
+    t.pos = reinterpret_cast<float4*>(base);
+    t.vel = t.pos + pbuf;
+    t.key = reinterpret_cast<uint32_t*>(t.vel + pbuf);
+    t.cell = reinterpret_cast<uint16_t*>(t.key + pbuf);
+    t.rank = t.cell + pbuf;
+    t.inv = t.rank + (algorithm ? pbuf : 0);
+    size_t at = (size_t)pbuf * (16 + 16 + 4 + 2 + (algorithm ? 4 : 0));
+    at = (at + 15) / 16 * 16;
+    uint32_t* u = reinterpret_cast<uint32_t*>(base + at);
+    t.cnt = u;
+    t.ng = u + (cells + 1);
+    t.off = u + 2 * (cells + 1);
+    t.goff = u + 3 * (cells + 1);
+    at = (at + 4 * (size_t)(cells + 1) * 4 + 15) / 16 * 16;
+    t.c0 = reinterpret_cast<float4*>(base + at);
+    t.c1 = t.c0 + cells;
+    t.omega = t.c1 + cells;
+    return t;
+}
+
+// Count of cell `c` of `tile` (first thread of the cell's group), zeroed as read
+// for reuse two steps later; issued one tile ahead so its latency hides.
+__device__ __forceinline__ uint32_t fetch_count(const StepArgs& a, uint32_t tile, uint32_t c, bool leader)
+{
+    if (!leader || tile >= a.num_tiles) return 0;
+    int bi;
+    const BoxDesc* bp = find_box(a, tile, bi);
+    const uint32_t c0 = (tile - bp->tile_base) * bp->tile_cells;
+    if (c >= min(bp->tile_cells, bp->C - c0)) return 0;
+    const uint32_t g = bp->cell_base + c0 + c;
+    const uint32_t raw = a.in_count[g];
+    a.in_count[g] = 0;
+    return raw;
+}
+
 // Overflow particles of step k (they found their bucket full when step k-1
-// scattered them): as in the reference, they stream but skip the collision,
-// and keep the unshifted position pbc(pbc(x + s) - s) (simulation_functions.cpp:90-93).
-__device__ void overflow_pass(const StepArgs& a, TileShared& sh)
+// scattered them): as in the reference, they stream but skip the collision and
+// keep the unshifted position pbc(pbc(x + s) - s) (simulation_functions.cpp:90-93).
+__device__ void overflow_pass(const StepArgs& a)
 {
     const unsigned parity = (unsigned)(a.step & 1);
-    if (threadIdx.x == 0) sh.ov_n = min(a.state->ov_count[parity], a.ov_cap);
-    __syncthreads();
-    const uint32_t n = sh.ov_n;
+    const uint32_t n = min(a.state->ov_count[parity], a.ov_cap);
     for (uint32_t base = 0; base < n; base += kThreads) {
         const uint32_t q = base + threadIdx.x;
         const bool active = q < n;
@@ -375,49 +440,70 @@ __device__ void overflow_pass(const StepArgs& a, TileShared& sh)
             const uint64_t lab = active ? (uint64_t)b.cell_base + ref_index(b, cell_of(b, x)) : 0;
             sample_add(a.samp, lab, v, active);
         }
-        scatter_particle(a, b, x, v, (uint32_t)(a.total_slots + q), id, sn, active);
+        scatter_particle(a, b, x, v, id, sn, active);
     }
     __syncthreads();
     if (threadIdx.x == 0) a.state->ov_count[parity] = 0;
 }
 
-template <int ALGO, bool TABLE>
+// Sum over the G lanes of a cell group (G a power of two dividing 32).
+template <class T>
+__device__ __forceinline__ T group_sum(T v, uint32_t G)
+{
+    for (uint32_t o = 1; o < G; o <<= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+template <int ALGO, bool TABLE, bool SINGLE>
 __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32_t pbuf)
 {
     using D = Draws<TABLE>;
     extern __shared__ __align__(128) unsigned char dyn[];
-    __shared__ TileShared sh;
-    float4* s_pos = reinterpret_cast<float4*>(dyn);
-    float4* s_vel = s_pos + pbuf;
-    uint16_t* s_cell = reinterpret_cast<uint16_t*>(s_vel + pbuf);
-    uint16_t* s_inv = s_cell + pbuf;
-    uint16_t* s_rank = s_inv + pbuf;
+    __shared__ uint32_t warp_tot[kThreads / 32 + 1];
+    __shared__ uint64_t bar;
     __shared__ BoxDesc sbox;
     __shared__ int sbox_index;
     __shared__ float3 sshift[2];
+    const uint32_t tcells = a.boxes_tile_cells;   // cells per tile, the same for every box of the launch
+    const TileLayout L = carve(dyn, pbuf, tcells, ALGO);
+    float4* const s_pos = L.pos;
+    float4* const s_vel = L.vel;
+    uint32_t* const s_key = L.key;
+    uint16_t* const s_cell = L.cell;
+    uint16_t* const s_rank = L.rank;   // extended only
+    uint16_t* const s_inv = L.inv;     // extended only
 
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
     if (tid == 0) {
-        mbar_init(&sh.bar);
-        sh.abort = 0;
+        mbar_init(&bar);
+        sbox_index = -1;
     }
     __syncthreads();
     uint32_t phase = 0;
 
-    if (blockIdx.x == 0) overflow_pass(a, sh);
+    if (blockIdx.x == 0) overflow_pass(a);
 
+    // group of G threads per cell (every box of a launch has the same tile size)
+    const uint32_t G = kThreads / tcells;
+    const uint32_t my_cell = (uint32_t)tid / G, my_j = (uint32_t)tid % G;
+    const bool leader = my_j == 0;
+
+    uint32_t next_raw = fetch_count(a, blockIdx.x, my_cell, leader);
     for (uint32_t tile = blockIdx.x; tile < a.num_tiles; tile += gridDim.x) {
         if (tid == 0) {
-            int bi;
-            const BoxDesc* bp = find_box(a, tile, bi);
-            sbox = *bp;
-            sbox_index = bi;
-            sshift[0] = grid_shift(*bp, bi, a.step, a.state);
-            sshift[1] = grid_shift(*bp, bi, a.step + 1, a.state);
+            int bi = 0;
+            const BoxDesc* bp = SINGLE ? &a.box0 : find_box(a, tile, bi);
+            if (bi != sbox_index) {   // box and its grid shifts change only between boxes
+                if (!SINGLE) sbox = *bp;
+                sbox_index = bi;
+                sshift[0] = grid_shift(*bp, bi, a.step, a.state);
+                sshift[1] = grid_shift(*bp, bi, a.step + 1, a.state);
+            }
         }
         __syncthreads();
-        const BoxDesc& b = sbox;
-        const int bi = sbox_index;
+        // single box: geometry straight from the kernel parameters (constant bank)
+        const BoxDesc& b = SINGLE ? a.box0 : sbox;
         const uint32_t c0 = (tile - b.tile_base) * b.tile_cells;
         const uint32_t nc = min(b.tile_cells, b.C - c0);
         const float3 s = sshift[0];
@@ -425,31 +511,49 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
         const float shift_abs = fabsf(s.z);
         const bool sign = s.z > 0;
 
-        // phase 0: counts (zeroed for reuse two steps later) and ghost counts
+        // counts (prefetched) and ghost counts, one group per cell
         uint32_t mine = 0, mine_g = 0;
-        if (tid < (int)nc) {
-            const uint32_t g = b.cell_base + c0 + tid;
-            const uint32_t raw = a.in_count[g];
-            a.in_count[g] = 0;
-            mine = min(raw, b.cap);
-            const uint3 cc = storage_coords(b, c0 + tid);
-            bool layer, ghosts;
-            wall_layer(b, cc.z, sign, layer, ghosts);
-            if (ghosts) mine_g = D::ghost_count(a, b, a.step, ref_index(b, cc), shift_abs, layer, sign);
-            sh.cnt[tid] = mine;
-            sh.ng[tid] = mine_g;
+        {
+            uint32_t gpart = 0;
+            if (my_cell < nc) {
+                const uint3 cc = storage_coords(b, c0 + my_cell);
+                bool layer, ghosts;
+                wall_layer(b, cc.z, sign, layer, ghosts);
+                if (ghosts) {
+                    const uint32_t ref = ref_index(b, cc);
+                    if (TABLE) {
+                        if (leader) gpart = D::ghost_count(a, b, a.step, ref, shift_abs, layer, sign);
+                    } else {
+                        for (uint32_t chunk = my_j; 4 * chunk < b.n; chunk += G) {   // 4 uniforms per Philox call
+                            const uint4 o = draw(b, a.step, kGhostCount, ref, chunk);
+                            const uint32_t u[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                                if (4 * chunk + k < b.n && ((u01(u[k]) > shift_abs) ^ layer ^ sign)) ++gpart;
+                        }
+                    }
+                }
+            }
+            gpart = group_sum(gpart, G);
+            if (leader && my_cell < nc) {
+                mine = min(next_raw, b.cap);
+                mine_g = gpart;
+                L.cnt[my_cell] = mine;
+                L.ng[my_cell] = mine_g;
+            }
         }
+        next_raw = fetch_count(a, tile + gridDim.x, my_cell, leader);
         uint32_t total;
-        const uint32_t off = block_exclusive_scan(mine + mine_g, sh.warp_tot, total);
+        const uint32_t off = block_exclusive_scan(mine + mine_g, warp_tot, total);
         uint32_t gtotal;
-        const uint32_t goff = block_exclusive_scan(mine_g, sh.warp_tot, gtotal);
-        if (tid < (int)nc) {
-            sh.off[tid] = off;
-            sh.goff[tid] = goff;
+        const uint32_t goff = block_exclusive_scan(mine_g, warp_tot, gtotal);
+        if (leader && my_cell < nc) {
+            L.off[my_cell] = off;
+            L.goff[my_cell] = goff;
         }
         if (tid == 0) {
-            sh.off[nc] = total;
-            sh.goff[nc] = gtotal;
+            L.off[nc] = total;
+            L.goff[nc] = gtotal;
         }
         __syncthreads();
 
@@ -459,236 +563,232 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
             uint32_t lo = i0 + 1, hi = nc;   // largest i1 with off[i1] - off[i0] <= pbuf
             while (lo < hi) {
                 const uint32_t mid = (lo + hi + 1) >> 1;
-                if (sh.off[mid] - sh.off[i0] <= pbuf) lo = mid; else hi = mid - 1;
+                if (L.off[mid] - L.off[i0] <= pbuf) lo = mid; else hi = mid - 1;
             }
             const uint32_t i1 = lo;
-            const uint32_t pbase = sh.off[i0];
-            const uint32_t np = sh.off[i1] - pbase;
+            const uint32_t pbase = L.off[i0];
+            const uint32_t np = L.off[i1] - pbase;
             if (np > pbuf) {   // impossible while 5n <= pbuf (checked on the host)
                 if (tid == 0) atomicOr(&a.state->error_flags, kErrKeyMismatch);
                 return;
             }
 
             // stage real particles: one bulk copy per cell and array
-            uint32_t real_bytes = 0;
-            for (uint32_t i = i0; i < i1; ++i) real_bytes += sh.cnt[i];   // all threads, smem broadcast
-            real_bytes *= 32u;
+            const uint32_t real_bytes = 32u * (np - (L.goff[i1] - L.goff[i0]));
             if (tid == 0 && real_bytes) {
                 fence_proxy_async();
-                mbar_arrive_expect_tx(&sh.bar, real_bytes);
+                mbar_arrive_expect_tx(&bar, real_bytes);
             }
             __syncthreads();
-            for (uint32_t i = i0 + tid; i < i1; i += kThreads) {
-                const uint32_t n = sh.cnt[i];
-                if (n) {
+            const bool in_sub = my_cell >= i0 && my_cell < i1;
+            if (in_sub) {
+                const uint32_t i = my_cell;
+                const uint32_t n = L.cnt[i];
+                const uint32_t o = L.off[i] - pbase, e = L.off[i + 1] - pbase;
+                if (leader && n) {
                     fence_proxy_async();
                     const uint64_t src = b.slot_base + (uint64_t)(c0 + i) * b.cap;
-                    const uint32_t dst = sh.off[i] - pbase;
-                    bulk_g2s(s_pos + dst, a.in_pos + src, n * 16u, &sh.bar);
-                    bulk_g2s(s_vel + dst, a.in_vel + src, n * 16u, &sh.bar);
+                    bulk_g2s(s_pos + o, a.in_pos + src, n * 16u, &bar);
+                    bulk_g2s(s_vel + o, a.in_vel + src, n * 16u, &bar);
                 }
-                // tile-local cell id of every staged particle, ghosts included
-                const uint32_t o = sh.off[i] - pbase, e = sh.off[i + 1] - pbase;
-                for (uint32_t p = o; p < e; ++p) s_cell[p] = (uint16_t)i;
+                for (uint32_t p = o + my_j; p < e; p += G) s_cell[p] = (uint16_t)i;
             }
             // ghosts, one thread per ghost (overlaps the copies)
             {
-                const uint32_t gb = sh.goff[i0], ge = sh.goff[i1];
+                const uint32_t gb = L.goff[i0], ge = L.goff[i1];
                 for (uint32_t q = gb + tid; q < ge; q += kThreads) {
                     uint32_t lo2 = i0, hi2 = i1 - 1;   // cell with goff[i] <= q < goff[i+1]
                     while (lo2 < hi2) {
                         const uint32_t mid = (lo2 + hi2 + 1) >> 1;
-                        if (sh.goff[mid] <= q) lo2 = mid; else hi2 = mid - 1;
+                        if (L.goff[mid] <= q) lo2 = mid; else hi2 = mid - 1;
                     }
-                    const uint32_t i = lo2, j = q - sh.goff[i];
+                    const uint32_t i = lo2, j = q - L.goff[i];
                     const uint3 cc = storage_coords(b, c0 + i);
                     bool layer, ghosts;
                     wall_layer(b, cc.z, sign, layer, ghosts);
                     float3 gx, gv;
                     D::ghost(a, b, a.step, ref_index(b, cc), j, cell_centre(b, cc), shift_abs, layer, sign, gx, gv);
-                    const uint32_t p = sh.off[i] - pbase + sh.cnt[i] + j;
+                    const uint32_t p = L.off[i] - pbase + L.cnt[i] + j;
                     s_pos[p] = make_float4(gx.x, gx.y, gx.z, 0.0f);
                     s_vel[p] = make_float4(gv.x, gv.y, gv.z, 0.0f);
                 }
             }
             if (real_bytes) {
                 int ok = 1;
-                if (tid == 0) ok = mbar_wait_bounded(&sh.bar, phase);
+                if (tid == 0) ok = mbar_wait_bounded(&bar, phase);
                 ok = __syncthreads_and(ok);
                 if (!ok) {
                     if (tid == 0) {
                         atomicOr(&a.state->error_flags, kErrWaitTimeout);
-                        mbar_wait_bounded(&sh.bar, phase);   // let copies in flight land
+                        mbar_wait_bounded(&bar, phase);   // let copies in flight land
                     }
                     return;
                 }
-                mbar_try_wait(&sh.bar, phase);   // completed phase: acquire for every thread
+                mbar_try_wait(&bar, phase);   // completed phase: acquire for every thread
                 phase ^= 1u;
             } else {
                 __syncthreads();
             }
 
-            // phase 3: stream step k (recomputed) and stable rank by prev key
+            // stream step k (recomputed); extended: rank by particle id
             for (uint32_t p = tid; p < np; p += kThreads) {
-                const uint32_t i = s_cell[p];
-                const uint32_t o = sh.off[i] - pbase;
+                const uint32_t ci = s_cell[p];
+                const uint32_t o = L.off[ci] - pbase;
                 const uint32_t r = p - o;
-                if (r < sh.cnt[i]) {
+                const uint32_t n = L.cnt[ci];
+                if (r < n) {
                     const float4 xp = s_pos[p], vp = s_vel[p];
                     float3 x = make_float3(xp.x, xp.y, xp.z), v = make_float3(vp.x, vp.y, vp.z);
                     x = stream_shift(b, x, v, s);
-                    const uint32_t key = __float_as_uint(xp.w);
-                    uint32_t rank = 0;   // ties (never expected) broken by staging order: always a permutation
-                    for (uint32_t q = 0; q < sh.cnt[i]; ++q) {
-                        const uint32_t kq = __float_as_uint(s_pos[o + q].w);
-                        rank += kq < key || (kq == key && q < r);
-                    }
-                    if (storage_index(b, cell_of(b, x)) != c0 + i) atomicOr(&a.state->error_flags, kErrKeyMismatch);
-                    s_rank[p] = (uint16_t)rank;
-                    s_inv[o + rank] = (uint16_t)p;
+                    s_pos[p] = make_float4(x.x, x.y, x.z, xp.w);
                     s_vel[p] = make_float4(v.x, v.y, v.z, vp.w);
-                    s_pos[p].x = x.x;
-                    s_pos[p].y = x.y;
-                    s_pos[p].z = x.z;
+                    if (ALGO == 1) {
+                        const uint32_t id = __float_as_uint(vp.w);
+                        uint32_t rank = 0;
+                        for (uint32_t q = 0; q < n; ++q) rank += __float_as_uint(s_vel[o + q].w) < id;
+                        s_rank[p] = (uint16_t)rank;
+                        s_inv[o + rank] = (uint16_t)p;
+                    }
                 }
             }
             __syncthreads();
 
-            // phase 5: one thread per cell
-            for (uint32_t i = i0 + tid; i < i1; i += kThreads) {
-                const uint32_t o = sh.off[i] - pbase, cnt = sh.cnt[i], g = sh.ng[i];
-                const uint3 cc = storage_coords(b, c0 + i);
-                const uint32_t ref = ref_index(b, cc);
-                if (ALGO == 0) {
-                    const uint32_t n = cnt + g;
+            // per-cell collision quantities, one group per cell
+            if (ALGO == 0) {
+                const uint32_t i = my_cell;
+                const uint32_t o = in_sub ? L.off[i] - pbase : 0;
+                const uint32_t n = in_sub ? L.cnt[i] + L.ng[i] : 0;
+                long long sx = 0, sy = 0, sz = 0;   // exact sums in units of 2^-32
+                for (uint32_t q = my_j; q < n; q += G) {
+                    const float4 vq = s_vel[o + q];
+                    sx += __float2ll_rn(vq.x * 4294967296.0f);
+                    sy += __float2ll_rn(vq.y * 4294967296.0f);
+                    sz += __float2ll_rn(vq.z * 4294967296.0f);
+                }
+                sx = group_sum(sx, G);
+                sy = group_sum(sy, G);
+                sz = group_sum(sz, G);
+                if (in_sub && leader) {
                     float3 mean = make_float3(0, 0, 0), axis = make_float3(0, 0, 0);
                     if (n > 1) {
-                        for (uint32_t r = 0; r < cnt; ++r) {
-                            const float4 w = s_vel[s_inv[o + r]];
-                            mean.x += w.x; mean.y += w.y; mean.z += w.z;
-                        }
-                        for (uint32_t j = 0; j < g; ++j) {
-                            const float4 w = s_vel[o + cnt + j];
-                            mean.x += w.x; mean.y += w.y; mean.z += w.z;
-                        }
                         const float inv = 1.0f / (float)n;
-                        mean.x *= inv; mean.y *= inv; mean.z *= inv;
-                        axis = D::srd_axis(a, b, a.step, ref);
+                        mean = make_float3((__ll2float_rn(sx) * 0x1p-32f) * inv, (__ll2float_rn(sy) * 0x1p-32f) * inv,
+                                           (__ll2float_rn(sz) * 0x1p-32f) * inv);
+                        axis = D::srd_axis(a, b, a.step, ref_index(b, storage_coords(b, c0 + i)));
                     }
-                    sh.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));
-                    sh.c1[i] = make_float4(axis.x, axis.y, axis.z, 0.0f);
-                } else {
-                    const uint32_t n = min(cnt + g, b.cap);
-                    const uint32_t m = n - g;   // real participants (leading ranks)
-                    float3 com = make_float3(0, 0, 0), mean = make_float3(0, 0, 0), omega = make_float3(0, 0, 0);
-                    if (n > 1) {
-                        const float3 centre = cell_centre(b, cc);
-                        float gate;
-                        const float3 axis = D::ext_axis(a, b, a.step, ref, gate);
-                        auto at = [&](uint32_t k) -> uint32_t { return k < m ? s_inv[o + k] : o + cnt + (k - m); };
-                        for (uint32_t k = 0; k < n; ++k) {
-                            const uint32_t p = at(k);
-                            const float4 xp = s_pos[p], vp = s_vel[p];
-                            com.x += (xp.x - centre.x); com.y += (xp.y - centre.y); com.z += (xp.z - centre.z);
-                            mean.x += vp.x; mean.y += vp.y; mean.z += vp.z;
-                        }
-                        const float inv = 1.0f / (float)n;
-                        com = make_float3(com.x * inv + centre.x, com.y * inv + centre.y, com.z * inv + centre.z);
-                        mean = make_float3(mean.x * inv, mean.y * inv, mean.z * inv);
-                        float proj0 = 0.0f;
-                        int size0 = 0;
-                        for (uint32_t k = 0; k < n; ++k) {
-                            const uint32_t p = at(k);
-                            float4 xp = s_pos[p], vp = s_vel[p];
-                            xp.x -= com.x; xp.y -= com.y; xp.z -= com.z;
-                            vp.x -= mean.x; vp.y -= mean.y; vp.z -= mean.z;
-                            s_pos[p] = xp;
-                            s_vel[p] = vp;
-                            if (dot3(make_float3(xp.x, xp.y, xp.z), axis) < 0) {
-                                proj0 += dot3(make_float3(vp.x, vp.y, vp.z), axis);
-                                size0 += 1;
-                            }
-                        }
-                        const int size1 = (int)n - size0;
-                        const float proj1 = -proj0 / (float)size1;
-                        proj0 = proj0 / (float)size0;
-                        const float prob = 1 - expf(0.01f * (proj1 - proj0) * (float)size0 * (float)size1);
-                        if (gate < prob) {
-                            const float t0 = proj1 * ((float)size1 / (float)size0);
-                            const float t1 = proj0 * ((float)size0 / (float)size1);
-                            float mean0 = 0.0f, mean1 = 0.0f;
-                            float I[6] = {0, 0, 0, 0, 0, 0};
-                            float3 dL = make_float3(0, 0, 0);
-                            for (uint32_t k = 0; k < n; ++k) {
-                                const uint32_t p = at(k);
-                                const float4 xp = s_pos[p];
-                                float4 vp = s_vel[p];
-                                const float3 x = make_float3(xp.x, xp.y, xp.z);
-                                float3 v = make_float3(vp.x, vp.y, vp.z);
-                                const bool side = dot3(x, axis) < 0;
-                                const float vr = D::thermal(a, b, a.step, ref, k) * b.tv;
-                                if (side) mean0 += vr; else mean1 += vr;
-                                const float3 cr = cross3(x, v);
-                                dL.x += cr.x; dL.y += cr.y; dL.z += cr.z;
-                                const float kick = (vr - dot3(v, axis)) + (side ? t0 : t1);
-                                v.x += axis.x * kick; v.y += axis.y * kick; v.z += axis.z * kick;
-                                s_vel[p] = make_float4(v.x, v.y, v.z, vp.w);
-                                const float sx = x.x * x.x, sy = x.y * x.y, sz = x.z * x.z;
-                                I[0] += sy + sz;
-                                I[1] += sx + sz;
-                                I[2] += sx + sy;
-                                I[3] += -x.x * x.y;
-                                I[4] += -x.x * x.z;
-                                I[5] += -x.y * x.z;
-                            }
-                            const float m0 = mean0 / (float)size0, m1 = mean1 / (float)size1;
-                            const float3 vm0 = make_float3(axis.x * m0, axis.y * m0, axis.z * m0);
-                            const float3 vm1 = make_float3(axis.x * m1, axis.y * m1, axis.z * m1);
-                            for (uint32_t k = 0; k < n; ++k) {
-                                const uint32_t p = at(k);
-                                const float4 xp = s_pos[p];
-                                float4 vp = s_vel[p];
-                                const float3 x = make_float3(xp.x, xp.y, xp.z);
-                                const float3 vm = dot3(x, axis) < 0 ? vm0 : vm1;
-                                vp.x -= vm.x; vp.y -= vm.y; vp.z -= vm.z;
-                                s_vel[p] = vp;
-                                const float3 cr = cross3(x, make_float3(vp.x, vp.y, vp.z));
-                                dL.x -= cr.x; dL.y -= cr.y; dL.z -= cr.z;
-                            }
-                            float Ii[6];
-                            sym_inverse(I, 1e-5f, Ii);
-                            omega = make_float3(Ii[0] * dL.x + Ii[3] * dL.y + Ii[4] * dL.z,
-                                                Ii[3] * dL.x + Ii[1] * dL.y + Ii[5] * dL.z,
-                                                Ii[4] * dL.x + Ii[5] * dL.y + Ii[2] * dL.z);
-                        }
-                    }
-                    sh.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));
-                    sh.c1[i] = make_float4(com.x, com.y, com.z, 0.0f);
-                    sh.c2[i] = make_float4(omega.x, omega.y, omega.z, __uint_as_float(m));
+                    L.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));
+                    L.c1[i] = make_float4(axis.x, axis.y, axis.z, 0.0f);
                 }
+            } else if (in_sub && leader) {
+                const uint32_t i = my_cell;
+                const uint32_t o = L.off[i] - pbase, cnt = L.cnt[i], g = L.ng[i];
+                const uint3 cc = storage_coords(b, c0 + i);
+                const uint32_t ref = ref_index(b, cc);
+                const uint32_t n = min(cnt + g, b.cap);
+                const uint32_t m = n - g;   // real participants (lowest ids)
+                float3 com = make_float3(0, 0, 0), mean = make_float3(0, 0, 0), omega = make_float3(0, 0, 0);
+                if (n > 1) {
+                    const float3 centre = cell_centre(b, cc);
+                    float gate;
+                    const float3 axis = D::ext_axis(a, b, a.step, ref, gate);
+                    auto at = [&](uint32_t k) -> uint32_t { return k < m ? s_inv[o + k] : o + cnt + (k - m); };
+                    for (uint32_t k = 0; k < n; ++k) {
+                        const uint32_t p = at(k);
+                        const float4 xp = s_pos[p], vp = s_vel[p];
+                        com.x += (xp.x - centre.x); com.y += (xp.y - centre.y); com.z += (xp.z - centre.z);
+                        mean.x += vp.x; mean.y += vp.y; mean.z += vp.z;
+                    }
+                    const float inv = 1.0f / (float)n;
+                    com = make_float3(com.x * inv + centre.x, com.y * inv + centre.y, com.z * inv + centre.z);
+                    mean = make_float3(mean.x * inv, mean.y * inv, mean.z * inv);
+                    float proj0 = 0.0f;
+                    int size0 = 0;
+                    for (uint32_t k = 0; k < n; ++k) {
+                        const uint32_t p = at(k);
+                        float4 xp = s_pos[p], vp = s_vel[p];
+                        xp.x -= com.x; xp.y -= com.y; xp.z -= com.z;
+                        vp.x -= mean.x; vp.y -= mean.y; vp.z -= mean.z;
+                        s_pos[p] = xp;
+                        s_vel[p] = vp;
+                        if (dot3(make_float3(xp.x, xp.y, xp.z), axis) < 0) {
+                            proj0 += dot3(make_float3(vp.x, vp.y, vp.z), axis);
+                            size0 += 1;
+                        }
+                    }
+                    const int size1 = (int)n - size0;
+                    const float proj1 = -proj0 / (float)size1;
+                    proj0 = proj0 / (float)size0;
+                    const float prob = 1 - expf(0.01f * (proj1 - proj0) * (float)size0 * (float)size1);
+                    if (gate < prob) {
+                        const float t0 = proj1 * ((float)size1 / (float)size0);
+                        const float t1 = proj0 * ((float)size0 / (float)size1);
+                        float mean0 = 0.0f, mean1 = 0.0f;
+                        float I[6] = {0, 0, 0, 0, 0, 0};
+                        float3 dL = make_float3(0, 0, 0);
+                        for (uint32_t k = 0; k < n; ++k) {
+                            const uint32_t p = at(k);
+                            const float4 xp = s_pos[p];
+                            float4 vp = s_vel[p];
+                            const float3 x = make_float3(xp.x, xp.y, xp.z);
+                            float3 v = make_float3(vp.x, vp.y, vp.z);
+                            const bool side = dot3(x, axis) < 0;
+                            const float vr = D::thermal(a, b, a.step, ref, k) * b.tv;
+                            if (side) mean0 += vr; else mean1 += vr;
+                            const float3 cr = cross3(x, v);
+                            dL.x += cr.x; dL.y += cr.y; dL.z += cr.z;
+                            const float kick = (vr - dot3(v, axis)) + (side ? t0 : t1);
+                            v.x += axis.x * kick; v.y += axis.y * kick; v.z += axis.z * kick;
+                            s_vel[p] = make_float4(v.x, v.y, v.z, vp.w);
+                            const float sx = x.x * x.x, sy = x.y * x.y, sz = x.z * x.z;
+                            I[0] += sy + sz;
+                            I[1] += sx + sz;
+                            I[2] += sx + sy;
+                            I[3] += -x.x * x.y;
+                            I[4] += -x.x * x.z;
+                            I[5] += -x.y * x.z;
+                        }
+                        const float m0 = mean0 / (float)size0, m1 = mean1 / (float)size1;
+                        const float3 vm0 = make_float3(axis.x * m0, axis.y * m0, axis.z * m0);
+                        const float3 vm1 = make_float3(axis.x * m1, axis.y * m1, axis.z * m1);
+                        for (uint32_t k = 0; k < n; ++k) {
+                            const uint32_t p = at(k);
+                            const float4 xp = s_pos[p];
+                            float4 vp = s_vel[p];
+                            const float3 x = make_float3(xp.x, xp.y, xp.z);
+                            const float3 vm = dot3(x, axis) < 0 ? vm0 : vm1;
+                            vp.x -= vm.x; vp.y -= vm.y; vp.z -= vm.z;
+                            s_vel[p] = vp;
+                            const float3 cr = cross3(x, make_float3(vp.x, vp.y, vp.z));
+                            dL.x -= cr.x; dL.y -= cr.y; dL.z -= cr.z;
+                        }
+                        float Ii[6];
+                        sym_inverse(I, 1e-5f, Ii);
+                        omega = make_float3(Ii[0] * dL.x + Ii[3] * dL.y + Ii[4] * dL.z,
+                                            Ii[3] * dL.x + Ii[1] * dL.y + Ii[5] * dL.z,
+                                            Ii[4] * dL.x + Ii[5] * dL.y + Ii[2] * dL.z);
+                    }
+                }
+                L.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));
+                L.c1[i] = make_float4(com.x, com.y, com.z, 0.0f);
+                L.omega[i] = make_float4(omega.x, omega.y, omega.z, __uint_as_float(m));
             }
             __syncthreads();
 
-            // phase 6: one thread per real particle: finish, sample, scatter
-            for (uint32_t base = 0; base < np; base += kThreads) {
-                const uint32_t p = base + tid;
+            // per particle: finish the collision, sample, find the next cell
+            for (uint32_t pb = 0; pb < np; pb += kThreads) {
+                const uint32_t p = pb + tid;
                 bool active = false;
-                uint32_t i = 0, r = 0;
+                uint32_t ci = 0;
                 if (p < np) {
-                    i = s_cell[p];
-                    r = p - (sh.off[i] - pbase);
-                    active = r < sh.cnt[i];
+                    ci = s_cell[p];
+                    active = p - (L.off[ci] - pbase) < L.cnt[ci];
                 }
                 float3 x = make_float3(0, 0, 0), v = make_float3(0, 0, 0);
-                uint32_t prev = 0, id = 0;
                 if (active) {
                     const float4 xp = s_pos[p], vp = s_vel[p];
                     x = make_float3(xp.x, xp.y, xp.z);
                     v = make_float3(vp.x, vp.y, vp.z);
-                    id = __float_as_uint(vp.w);
-                    const uint32_t rank = s_rank[p];
-                    prev = (uint32_t)(b.slot_base + (uint64_t)(c0 + i) * b.cap + rank);
-                    const float4 k0 = sh.c0[i], k1 = sh.c1[i];
+                    const float4 k0 = L.c0[ci], k1 = L.c1[ci];
                     const uint32_t n = __float_as_uint(k0.w);
                     const float3 mean = make_float3(k0.x, k0.y, k0.z);
                     if (ALGO == 0) {
@@ -707,9 +807,9 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                             v.x += b.drag_dt;
                         }
                     } else {
-                        const float4 k2 = sh.c2[i];
+                        const float4 k2 = L.omega[ci];
                         const uint32_t m = __float_as_uint(k2.w);
-                        if (n > 1 && rank < m) {
+                        if (n > 1 && s_rank[p] < m) {
                             const float3 com = make_float3(k1.x, k1.y, k1.z);
                             const float3 omega = make_float3(k2.x, k2.y, k2.z);
                             v.x += mean.x; v.y += mean.y; v.z += mean.z;
@@ -719,12 +819,61 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                             x = pbc(b, make_float3((com.x + x.x) - s.x, (com.y + x.y) - s.y, (com.z + x.z) - s.z));
                         }
                     }
+                    float3 vn = v;
+                    const float3 xn = stream_shift(b, x, vn, sn);
+                    s_key[p] = b.cell_base + storage_index(b, cell_of(b, xn));
+                    s_pos[p] = make_float4(x.x, x.y, x.z, 0.0f);
+                    s_vel[p] = make_float4(v.x, v.y, v.z, vp.w);
+                } else if (p < np) {
+                    s_key[p] = kNoKey;
                 }
                 if (a.sample) {
                     const uint64_t lab = active ? (uint64_t)b.cell_base + ref_index(b, cell_of(b, x)) : 0;
                     sample_add(a.samp, lab, v, active);
                 }
-                scatter_particle(a, b, x, v, prev, id, sn, active);
+            }
+            __syncthreads();
+
+            // claim bucket slots (warp-aggregated atomics, all issued before any
+            // result is used), then write the particles to their buckets
+            {
+                uint32_t key[kMaxPerThread], peers[kMaxPerThread], base[kMaxPerThread];
+#pragma unroll
+                for (int j = 0; j < kMaxPerThread; ++j) {
+                    const uint32_t p = (uint32_t)tid + (uint32_t)kThreads * j;
+                    key[j] = p < np ? s_key[p] : kNoKey;
+                    const bool act = key[j] != kNoKey;
+                    const unsigned m = __ballot_sync(kFull, act);
+                    peers[j] = 0;
+                    base[j] = 0;
+                    if (act) {
+                        peers[j] = __match_any_sync(m, key[j]);
+                        if (lane == __ffs(peers[j]) - 1) base[j] = atomicAdd(a.out_count + key[j], __popc(peers[j]));
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < kMaxPerThread; ++j) {
+                    if (key[j] == kNoKey) continue;
+                    const uint32_t p = (uint32_t)tid + (uint32_t)kThreads * j;
+                    const uint32_t slot =
+                        __shfl_sync(peers[j], base[j], __ffs(peers[j]) - 1) + __popc(peers[j] & lanemask_lt());
+                    const float4 xp = s_pos[p], vp = s_vel[p];
+                    if (slot < b.cap) {
+                        const uint64_t at = b.slot_base + (uint64_t)(key[j] - b.cell_base) * b.cap + slot;
+                        a.out_pos[at] = xp;
+                        a.out_vel[at] = vp;
+                    } else {
+                        atomicAdd(&a.state->overflow_total, 1ull);
+                        const unsigned parity = (unsigned)((a.step + 1) & 1);
+                        const unsigned q = atomicAdd(&a.state->ov_count[parity], 1u);
+                        if (q < a.ov_cap) {
+                            a.ov_out_pos[q] = xp;
+                            a.ov_out_vel[q] = vp;
+                        } else {
+                            atomicOr(&a.state->error_flags, kErrOverflowListFull);
+                        }
+                    }
+                }
             }
             __syncthreads();
             i0 = i1;
@@ -752,7 +901,7 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(StepArgs a, const flo
             v = make_float3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
             s = grid_shift(a.boxes[bi], bi, a.step + 1, a.state);
         }
-        scatter_particle(a, a.boxes[bi], x, v, (uint32_t)i, (uint32_t)i, s, active);
+        scatter_particle(a, a.boxes[bi], x, v, (uint32_t)i, s, active);
     }
 }
 
@@ -877,10 +1026,10 @@ __global__ void __launch_bounds__(kThreads) compact_kernel(const StepArgs a, con
         const uint32_t dst0 = offsets[c];
         const uint32_t ref = ref_index(b, storage_coords(b, (uint32_t)(c - b.cell_base)));
         for (uint32_t q = 0; q < n; ++q) {
-            const uint32_t key = __float_as_uint(pos[slot0 + q].w);
+            const uint32_t key = __float_as_uint(vel[slot0 + q].w);   // particle id
             uint32_t rank = 0;
             for (uint32_t u = 0; u < n; ++u) {
-                const uint32_t ku = __float_as_uint(pos[slot0 + u].w);
+                const uint32_t ku = __float_as_uint(vel[slot0 + u].w);
                 rank += ku < key || (ku == key && u < q);
             }
             const uint64_t d = (uint64_t)dst0 + rank;
@@ -916,7 +1065,7 @@ __global__ void compact_overflow_kernel(const BoxDesc* boxes, int nboxes, uint64
             out_cell[d] = b.cell_base + ref_index(b, cell_of(b, xs));
         }
         if (out_slot) out_slot[d] = (uint32_t)(total_slots + q);
-        if (out_prev) out_prev[d] = __float_as_uint(ov_pos[q].w);
+        if (out_prev) out_prev[d] = __float_as_uint(ov_vel[q].w);
         if (out_id) out_id[d] = __float_as_uint(ov_vel[q].w);
     }
 }
@@ -1036,28 +1185,34 @@ __global__ void subtract_kernel(float* vel, uint64_t begin, uint64_t end, float 
 
 // ------------------------------------------------------------------ launchers
 
-size_t step_smem_bytes(uint32_t pbuf) { return (size_t)pbuf * (16 + 16 + 2 + 2 + 2); }
+size_t step_smem_bytes(uint32_t pbuf, uint32_t cells, int algorithm) { return tile_smem_bytes(pbuf, cells, algorithm); }
+
+namespace {
+using StepFn = void (*)(const StepArgs, uint32_t);
+constexpr StepFn kStepFns[2][2][2] = {
+    {{step_kernel<0, false, false>, step_kernel<0, false, true>}, {step_kernel<0, true, false>, step_kernel<0, true, true>}},
+    {{step_kernel<1, false, false>, step_kernel<1, false, true>}, {step_kernel<1, true, false>, step_kernel<1, true, true>}}};
+}  // namespace
 
 cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st)
 {
-    const size_t smem = step_smem_bytes(pbuf);
-    if (algorithm == 0 && !table) step_kernel<0, false><<<grid, kThreads, smem, st>>>(a, pbuf);
-    else if (algorithm == 0) step_kernel<0, true><<<grid, kThreads, smem, st>>>(a, pbuf);
-    else if (!table) step_kernel<1, false><<<grid, kThreads, smem, st>>>(a, pbuf);
-    else step_kernel<1, true><<<grid, kThreads, smem, st>>>(a, pbuf);
+    const size_t smem = step_smem_bytes(pbuf, a.boxes_tile_cells, algorithm);
+    kStepFns[algorithm ? 1 : 0][table ? 1 : 0][a.nboxes == 1 ? 1 : 0]<<<grid, kThreads, smem, st>>>(a, pbuf);
     return cudaGetLastError();
 }
 
-cudaError_t configure_step(int algorithm, uint32_t pbuf, int* blocks_per_sm)
+cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* blocks_per_sm)
 {
-    const size_t smem = step_smem_bytes(pbuf);
-    const void* fns[4] = {(const void*)step_kernel<0, false>, (const void*)step_kernel<0, true>,
-                          (const void*)step_kernel<1, false>, (const void*)step_kernel<1, true>};
-    for (const void* f : fns) {
-        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fns[algorithm ? 2 : 0], kThreads, smem);
+    const size_t smem = step_smem_bytes(pbuf, cells, algorithm);
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j)
+            for (int k = 0; k < 2; ++k) {
+                cudaError_t e = cudaFuncSetAttribute((const void*)kStepFns[i][j][k],
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e != cudaSuccess) return e;
+            }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, (const void*)kStepFns[algorithm ? 1 : 0][0][1],
+                                                         kThreads, smem);
 }
 
 cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel, uint64_t n_total, int grid,

@@ -9,10 +9,11 @@
 
 namespace mpcd_gb {
 
-// Dynamic shared memory of the step kernel for a particle buffer of `pbuf` entries.
-size_t step_smem_bytes(uint32_t pbuf);
-// Opt the step kernels into `pbuf` and report resident CTAs per SM.
-cudaError_t configure_step(int algorithm, uint32_t pbuf, int* blocks_per_sm);
+// Dynamic shared memory of the step kernel: a particle buffer of `pbuf`
+// entries and tiles of `cells` cells.
+size_t step_smem_bytes(uint32_t pbuf, uint32_t cells, int algorithm);
+// Opt the step kernels into that much shared memory and report resident CTAs per SM.
+cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* blocks_per_sm);
 // One step of every box (algorithm 0 = SRD, 1 = extended; table = injected draws).
 cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st);
 // Key dense clean particles for step a.step + 1 and scatter them into a.out_*.

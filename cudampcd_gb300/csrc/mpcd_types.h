@@ -14,7 +14,6 @@
 namespace mpcd_gb {
 
 constexpr int kThreads = 256;        // threads per CTA of the step kernel
-constexpr int kMaxTileCells = 128;   // cells per tile, upper bound
 constexpr int kMaxInjectedShifts = 4;
 
 // One simulation box (a "replica" in a batched ensemble).
@@ -77,8 +76,10 @@ struct DrawTables {
 };
 
 struct StepArgs {
+    BoxDesc box0;                 // the only box of a single-box launch (kernel-parameter space)
     const BoxDesc* boxes;
     int32_t nboxes;
+    uint32_t boxes_tile_cells;    // cells per tile (the same for every box of a launch)
     uint32_t num_tiles;
     uint64_t total_slots;
     uint64_t step;                // k: this launch completes step k

@@ -129,15 +129,14 @@ int32_t mpcd_gb_inject_shift(mpcd_gb_handle *h, uint64_t step, const float shift
 int32_t mpcd_gb_get_shift(mpcd_gb_handle *h, uint64_t step, float shift[3]);
 
 /* Layout of the current cell buckets -- the counting sort by cell -- one entry
- * per particle in layout order (cells in storage order z fastest, then x, then
- * y; stable order within a cell; then particles waiting in the overflow list):
- * cell = reference cell index x + Lx*(y + Ly*z) of the bucket, slot = sparse
- * slot id, prev = position in the previous layout (slot id, or the index into
- * the arrays given to a setter), id = particle id.  counts: C entries
- * (reference cell order), the number of particles each cell received, overflow
- * included (the reference's uniform_counter).  Any pointer may be NULL. */
-int32_t mpcd_gb_dump_layout(mpcd_gb_handle *h, uint32_t *cell, uint32_t *slot, uint32_t *prev, uint32_t *id,
-                            uint32_t *counts);
+ * per particle in layout order: cells in storage order (z fastest, then x, then
+ * y), within a cell ascending particle id (the stable sort of the id-ordered
+ * particle array by cell), then the particles waiting in the overflow list
+ * ordered by (cell, id).  cell = reference cell index x + Lx*(y + Ly*z) the
+ * particle is keyed to, slot = its sparse slot id, id = particle id.  counts: C
+ * entries (reference cell order), the number of particles each cell received,
+ * overflow included (the reference's uniform_counter).  Any pointer may be NULL. */
+int32_t mpcd_gb_dump_layout(mpcd_gb_handle *h, uint32_t *cell, uint32_t *slot, uint32_t *id, uint32_t *counts);
 
 /* Injected draws for the next step (the oracle's recorded tables, reference
  * cell order): ghost_count[C], ghost_pos[C*gmax*3], ghost_vel[C*gmax*3],

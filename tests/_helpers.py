@@ -23,7 +23,7 @@ def storage_keys(box: O.Box, ref_cells: np.ndarray) -> np.ndarray:
 
 def set_state(h: capi.Handle, pos, vel, shift=None):
     """Load a dense state (particle id = row), optionally with the grid shift of
-    the next step injected; returns the resulting layout (cell, slot, prev, id, counts)."""
+    the next step injected; returns the resulting layout (cell, slot, id, counts)."""
     if shift is not None:
         h.inject_shift(h.step_index, shift)
     h.set_particles(pos, vel)

@@ -39,16 +39,15 @@ def test_stream_keys_counts_permutation_bit_exact(name, shift):
     box = BOXES[name]
     h = make(box, seed=11)
     pos, vel, _ = O.distribute(box, h.N, 3, 4)
-    cell, slot, prev, pid, counts = set_state(h, pos, vel, shift)
+    cell, slot, pid, counts = set_state(h, pos, vel, shift)
     tp, tv, tc, counter, _ = O.translate(box, pos, vel, np.float32(shift))
     assert np.array_equal(counts, counter)
-    # every particle of the layout sits in the reference's cell of its dense index
-    assert np.array_equal(pid, prev)
-    assert np.array_equal(cell, tc[prev])
-    # the layout is the stable sort of the dense array by storage cell
+    # every particle of the layout sits in the reference's cell of its index
+    assert np.array_equal(cell, tc[pid])
+    # the layout is the stable sort of the (id-ordered) array by storage cell
     assert counts.max() <= 4 * box.n, "test configuration must not overflow a cell"
     perm = O.stable_perm(O.storage_index(box, tc), box.C)
-    assert np.array_equal(prev, perm)
+    assert np.array_equal(pid, perm)
     # the clean state is stored unchanged and read back by particle id
     assert np.array_equal(h.positions(), pos) and np.array_equal(h.velocities(), vel)
     h.close()
@@ -63,14 +62,14 @@ def test_translate_known_answer():
     box = O.Box(L=(10, 10, 10), periodic=(1, 1, 1), n=10, dt=1.0)
     h = make(box)
     v = O.xoshiro_sequence(42, 43, 3, h.N)
-    cell, _, prev, _, counts = set_state(h, np.zeros((h.N, 3), np.float32), v, (0, 0, 0))
-    assert np.array_equal(cell, O.cell_index(box, v[prev]))   # after dt = 1 the position equals the velocity
+    cell, _, pid, counts = set_state(h, np.zeros((h.N, 3), np.float32), v, (0, 0, 0))
+    assert np.array_equal(cell, O.cell_index(box, v[pid]))   # after dt = 1 the position equals the velocity
     _, _, _, counter, _ = O.translate(box, np.zeros((h.N, 3), np.float32), v, (0, 0, 0))
     assert np.array_equal(counts, counter)
     # all particles at (-5, -5, -5) with zero velocity land in cell 0
     h.inject_shift(h.step_index, (0, 0, 0))
     h.set_particles(np.full((h.N, 3), -5.0, np.float32), np.zeros((h.N, 3), np.float32))
-    counts = h.layout()[4]
+    counts = h.layout()[3]
     assert counts[0] == h.N and counts[1:].sum() == 0
     overflowed, flags = h.counters()
     assert overflowed >= h.N - 4 * box.n and flags == 0
@@ -80,7 +79,7 @@ def test_translate_known_answer():
 def _collide_with_reference_draws(box, shift0, shift1, seed_a, seed_b):
     h = make(box, seed=99)
     pos, vel, _ = O.distribute(box, h.N, seed_a, seed_b)
-    _, slot_in, prev_in, id_in, _ = set_state(h, pos, vel, shift0)
+    set_state(h, pos, vel, shift0)
     tp, tv, tc, counter, table = O.translate(box, pos, vel, np.float32(shift0))
     draws = O.Draws.empty(box)
     op, ov, oc = O.collide(box, tp, tv, tc, counter, table, np.float32(shift0), draws, O.DRAWS_XOSHIRO,
@@ -89,11 +88,11 @@ def _collide_with_reference_draws(box, shift0, shift1, seed_a, seed_b):
     h.inject_draws(draws)
     h.step(1)
     gp, gv = h.positions(), h.velocities()
-    cell_out, _, prev_out, id_out, counts_out = h.layout()
-    # the new layout is keyed by the cell after streaming the next step and is the
-    # stable sort, by that cell, of the previous layout
+    cell_out, _, id_out, counts_out = h.layout()
+    # the new layout is keyed by the cell after streaming the next step: the
+    # stable sort of the id-ordered collided state by that cell
     _, _, nc, ncount, _ = O.translate(box, op, ov, np.float32(shift1))
-    expect = id_in[O.stable_perm(O.storage_index(box, nc[id_in]), box.C)]
+    expect = O.stable_perm(O.storage_index(box, nc), box.C)
     h.close()
     return dict(pos=pos, vel=vel, gp=gp, gv=gv, op=op, ov=ov, draws=draws, tc=tc, tv=tv, nc=nc,
                 ncount=ncount, counts_out=counts_out, id_out=id_out, expect=expect, cell_out=cell_out)
@@ -120,10 +119,13 @@ def test_collision_matches_reference_draws(name, seeds):
     assert np.array_equal(r["cell_out"], r["nc"][r["id_out"]])
 
 
-def test_srd_collision_is_bit_exact_with_reference_draws():
+def test_srd_collision_at_fp32_rounding_of_reference_draws():
+    """The SRD cell mean is an exact fixed-point sum rounded once; the reference
+    sums in float in index order.  They differ by a few ulp at most."""
     box = BOXES["srd_walls_dense"]
     r = _collide_with_reference_draws(box, SHIFTS[2], SHIFTS[0], 21, 22)
-    assert np.array_equal(r["gv"], r["ov"])
+    assert np.array_equal(r["gp"], r["op"])
+    assert rel_err(r["gv"], r["ov"], box.thermal_velocity).max() <= 2e-6
 
 
 @pytest.mark.parametrize("name", ["srd_periodic", "srd_walls", "ext_periodic", "ext_walls", "channel"])
