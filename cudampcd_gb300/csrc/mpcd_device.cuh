@@ -117,11 +117,19 @@ __device__ __forceinline__ uint32_t storage_index(const BoxDesc& b, uint3 c)
     return c.z + (uint32_t)b.L[2] * (c.x + (uint32_t)b.L[0] * c.y);
 }
 
+// n / d for n < 2^31, d <= 2^16, with m = ceil(2^48 / d): floor(n m / 2^48)
+// (the error n (m - 2^48/d) / 2^48 < 2^-17 stays below 1/d)
+__device__ __forceinline__ uint32_t fast_div(uint32_t n, uint64_t m)
+{
+    return (uint32_t)__umul64hi((uint64_t)n << 16, m);
+}
+
 __device__ __forceinline__ uint3 storage_coords(const BoxDesc& b, uint32_t s)
 {
     const uint32_t Lz = (uint32_t)b.L[2], Lx = (uint32_t)b.L[0];
-    const uint32_t z = s % Lz, col = s / Lz;
-    return make_uint3(col % Lx, col / Lx, z);
+    const uint32_t col = fast_div(s, b.div_z), z = s - col * Lz;
+    const uint32_t y = fast_div(col, b.div_x), x = col - y * Lx;
+    return make_uint3(x, y, z);
 }
 
 // centre of a cell in the shifted frame (volume_container.hpp:347-352)

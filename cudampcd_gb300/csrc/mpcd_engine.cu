@@ -17,7 +17,7 @@
 
 #include <cuda_runtime.h>
 
-#include "../../include/mpcd_gb.h"
+#include "mpcd_gb.h"
 #include "mpcd_kernels.h"
 
 namespace mpcd_gb {
@@ -163,7 +163,7 @@ public:
 
     void get(float* pos, float* vel)
     {
-        gather(dense_pos_.as<float>(), dense_vel_.as<float>());
+        materialise();
         if (pos)
             check(cudaMemcpyAsync(pos, dense_pos_.p, sizeof(float) * 3 * N_, cudaMemcpyDeviceToHost, stream_),
                   "positions read");
@@ -175,7 +175,7 @@ public:
 
     void set(const float* pos, const float* vel)
     {
-        if (!pos || !vel) gather(dense_pos_.as<float>(), dense_vel_.as<float>());
+        if (!pos || !vel) materialise();
         if (pos)
             check(cudaMemcpyAsync(dense_pos_.p, pos, sizeof(float) * 3 * N_, cudaMemcpyHostToDevice, stream_),
                   "positions write");
@@ -205,7 +205,7 @@ public:
         if (id) std::copy(hi.begin(), hi.end(), id);
         if (counts) {
             std::vector<uint32_t> raw(cells_);
-            check(cudaMemcpyAsync(raw.data(), count_[parity()].p, sizeof(uint32_t) * cells_, cudaMemcpyDeviceToHost,
+            check(cudaMemcpyAsync(raw.data(), count_[step_ % 3].p, sizeof(uint32_t) * cells_, cudaMemcpyDeviceToHost,
                                   stream_),
                   "dump");
             check(cudaStreamSynchronize(stream_), "dump");
@@ -225,7 +225,7 @@ public:
     {
         DeviceState st;
         check(cudaMemcpy(&st, state_.p, sizeof st, cudaMemcpyDeviceToHost), "dump");
-        const uint64_t m = std::min(st.ov_count[parity()], ov_cap_);
+        const uint64_t m = std::min(st.ov_count[step_ % 3], ov_cap_);
         if (m < 2) return;
         const uint64_t base = N_ - m;
         std::vector<uint64_t> order(m);
@@ -399,6 +399,8 @@ private:
         b.cell_base = 0;
         b.slot_base = 0;
         b.dense_base = 0;
+        b.div_z = ((1ull << 48) + (uint64_t)b.L[2] - 1) / (uint64_t)b.L[2];
+        b.div_x = ((1ull << 48) + (uint64_t)b.L[0] - 1) / (uint64_t)b.L[0];
         b.seed_lo = (uint32_t)p.seed;
         b.seed_hi = (uint32_t)(p.seed >> 32);
         // tile: a power-of-two number of cells (a group of 256 / cells threads per
@@ -454,10 +456,12 @@ private:
         for (int k = 0; k < 2; ++k) {
             check(pos_[k].alloc(sizeof(float4) * total_slots_), "alloc bucket positions");
             check(vel_[k].alloc(sizeof(float4) * total_slots_), "alloc bucket velocities");
-            check(count_[k].alloc(sizeof(uint32_t) * cells_), "alloc counts");
-            check(cudaMemset(count_[k].p, 0, count_[k].bytes), "clear counts");
             check(ov_pos_[k].alloc(sizeof(float4) * ov_cap_), "alloc overflow list");
             check(ov_vel_[k].alloc(sizeof(float4) * ov_cap_), "alloc overflow list");
+        }
+        for (int k = 0; k < 3; ++k) {
+            check(count_[k].alloc(sizeof(uint32_t) * cells_), "alloc counts");
+            check(cudaMemset(count_[k].p, 0, count_[k].bytes), "clear counts");
         }
         check(state_.alloc(sizeof(DeviceState)), "alloc state");
         check(cudaMemset(state_.p, 0, sizeof(DeviceState)), "clear state");
@@ -505,7 +509,10 @@ private:
         check_device_errors();
     }
 
-    StepArgs args() const
+    // Arguments of the launch that completes step k: buckets by parity k & 1,
+    // counts and overflow fill by k % 3 (the inputs of step k survive step k,
+    // so that a replay can recompute its collision).
+    StepArgs args(uint64_t k, bool replay = false) const
     {
         StepArgs a{};
         a.box0 = boxes_[0];
@@ -514,77 +521,84 @@ private:
         a.boxes_tile_cells = boxes_[0].tile_cells;
         a.num_tiles = (uint32_t)tiles_;
         a.total_slots = total_slots_;
-        a.step = step_;
-        const unsigned p = parity(), q = p ^ 1u;
+        a.step = k;
+        const unsigned p = (unsigned)(k & 1), q = p ^ 1u;
         a.in_pos = pos_[p].as<float4>();
         a.in_vel = vel_[p].as<float4>();
-        a.in_count = count_[p].as<uint32_t>();
+        a.in_count = count_[k % 3].as<uint32_t>();
         a.out_pos = pos_[q].as<float4>();
         a.out_vel = vel_[q].as<float4>();
-        a.out_count = count_[q].as<uint32_t>();
+        a.out_count = count_[(k + 1) % 3].as<uint32_t>();
+        a.zero_count = count_[(k + 2) % 3].as<uint32_t>();
         a.ov_in_pos = ov_pos_[p].as<float4>();
         a.ov_in_vel = ov_vel_[p].as<float4>();
         a.ov_out_pos = ov_pos_[q].as<float4>();
         a.ov_out_vel = ov_vel_[q].as<float4>();
         a.ov_cap = ov_cap_;
+        a.ov_in_slot = (uint32_t)(k % 3);
+        a.ov_out_slot = (uint32_t)((k + 1) % 3);
+        a.ov_zero_slot = (uint32_t)((k + 2) % 3);
         a.state = state_.as<DeviceState>();
         a.samp = samp_.as<float4>();
         std::memcpy(a.ext_axis, ext_axis_, sizeof ext_axis_);
         a.draws = tables_;
+        a.replay = replay ? 1 : 0;
+        a.dense_pos = dense_pos_.as<float>();
+        a.dense_vel = dense_vel_.as<float>();
         return a;
     }
 
     void launch_one_step(bool sample)
     {
-        StepArgs a = args();
+        StepArgs a = args(step_);
         a.sample = sample ? 1 : 0;
         check(launch_step(a, params_.algorithm, use_table_, pbuf_, grid_, stream_), "step kernel");
+        last_step_table_ = use_table_;   // a replay of this step must consume the same draws
         use_table_ = false;
         ++step_;
+        dense_valid_ = false;
     }
 
-    // Dense clean arrays -> buckets of the current parity (state before step step_).
+    // The post-step state, by particle id, in dense_pos_ / dense_vel_: recompute
+    // the collision of the last step from its inputs (same draws, same
+    // arithmetic, bit-identical) unless the dense arrays already hold it.
+    void materialise()
+    {
+        if (!dense_valid_) {
+            if (step_ == 0) throw Error(MPCD_GB_ESTATE, "no state to read");
+            StepArgs a = args(step_ - 1, true);
+            check(launch_step(a, params_.algorithm, last_step_table_, pbuf_, grid_, stream_), "replay");
+            check(cudaStreamSynchronize(stream_), "replay");
+            check_device_errors();
+            dense_valid_ = true;
+        }
+    }
+
+    // Dense post-step arrays (dense_pos_, dense_vel_) -> buckets of step step_:
+    // the scatter plays the epilogue of step step_ - 1.
     void scatter_dense()
     {
-        const unsigned p = parity();
-        check(cudaMemsetAsync(count_[p].p, 0, count_[p].bytes, stream_), "clear counts");
-        check(cudaMemsetAsync((char*)state_.p + offsetof(DeviceState, ov_count) + sizeof(unsigned int) * p, 0,
-                              sizeof(unsigned int), stream_),
-              "clear overflow list");
-        StepArgs a = args();
-        a.step = step_ - 1;   // the scatter plays the epilogue of the previous step
-        a.out_pos = pos_[p].as<float4>();
-        a.out_vel = vel_[p].as<float4>();
-        a.out_count = count_[p].as<uint32_t>();
-        a.ov_out_pos = ov_pos_[p].as<float4>();
-        a.ov_out_vel = ov_vel_[p].as<float4>();
+        const uint64_t k = step_;
+        for (uint64_t j = k; j < k + 2; ++j) {
+            check(cudaMemsetAsync(count_[j % 3].p, 0, count_[j % 3].bytes, stream_), "clear counts");
+            check(cudaMemsetAsync((char*)state_.p + offsetof(DeviceState, ov_count) + sizeof(unsigned int) * (j % 3),
+                                  0, sizeof(unsigned int), stream_),
+                  "clear overflow list");
+        }
+        StepArgs a = args(k - 1);   // out_* = buckets, counts and overflow list of step k
         check(launch_scatter(a, dense_pos_.as<float>(), dense_vel_.as<float>(), N_, sms_ * 8, stream_),
               "scatter");
-    }
-
-    void gather(float* pos, float* vel)
-    {
-        const unsigned p = parity();
-        StepArgs a = args();
-        check(cudaMemsetAsync(scan_counter_.p, 0, sizeof(unsigned int), stream_), "gather");
-        check(launch_gather(a, count_[p].as<uint32_t>(), pos_[p].as<float4>(), vel_[p].as<float4>(), cells_, N_,
-                            ov_pos_[p].as<float4>(), ov_vel_[p].as<float4>(), p, pos, vel,
-                            scan_counter_.as<unsigned int>(), sms_ * 8, stream_),
-              "gather");
-        unsigned int seen = 0;
-        check(cudaMemcpyAsync(&seen, scan_counter_.p, sizeof seen, cudaMemcpyDeviceToHost, stream_), "gather");
-        check(cudaStreamSynchronize(stream_), "gather");
-        expect_count(seen);
+        dense_valid_ = true;
     }
 
     void layout(uint32_t* cell, uint32_t* slot, uint32_t* prev, uint32_t* id)
     {
         const unsigned p = parity();
-        StepArgs a = args();
-        check(launch_layout(a, count_[p].as<uint32_t>(), pos_[p].as<float4>(), vel_[p].as<float4>(),
+        StepArgs a = args(step_);
+        check(launch_layout(a, count_[step_ % 3].as<uint32_t>(), pos_[p].as<float4>(), vel_[p].as<float4>(),
                             offsets_.as<uint32_t>(), cells_, N_, scan_status_.as<unsigned long long>(),
-                            scan_counter_.as<unsigned int>(), ov_pos_[p].as<float4>(), ov_vel_[p].as<float4>(), p,
-                            cell, slot, prev, id, sms_ * 8, stream_),
+                            scan_counter_.as<unsigned int>(), ov_pos_[p].as<float4>(), ov_vel_[p].as<float4>(),
+                            (unsigned)(step_ % 3), cell, slot, prev, id, sms_ * 8, stream_),
               "layout");
         uint32_t total = 0;
         check(cudaMemcpyAsync(&total, offsets_.as<uint32_t>() + cells_, sizeof total, cudaMemcpyDeviceToHost, stream_),
@@ -592,7 +606,7 @@ private:
         DeviceState st;
         check(cudaMemcpyAsync(&st, state_.p, sizeof st, cudaMemcpyDeviceToHost, stream_), "layout");
         check(cudaStreamSynchronize(stream_), "layout");
-        expect_count((uint64_t)total + std::min(st.ov_count[p], ov_cap_));
+        expect_count((uint64_t)total + std::min(st.ov_count[step_ % 3], ov_cap_));
     }
 
     void expect_count(uint64_t have)
@@ -645,11 +659,13 @@ private:
     bool sampling_ = false;
     uint64_t sample_counter_ = 0;
     bool use_table_ = false;
+    bool last_step_table_ = false;
+    bool dense_valid_ = false;   // dense_pos_ / dense_vel_ hold the state after step step_ - 1
     DrawTables tables_{};
     int inject_valid_[kMaxInjectedShifts] = {0, 0, 0, 0};
     uint64_t inject_step_[kMaxInjectedShifts] = {0, 0, 0, 0};
     float inject_shift_[kMaxInjectedShifts][3] = {};
-    DeviceBuffer boxes_d_, pos_[2], vel_[2], count_[2], ov_pos_[2], ov_vel_[2], state_, samp_, acc_, dense_pos_,
+    DeviceBuffer boxes_d_, pos_[2], vel_[2], count_[3], ov_pos_[2], ov_vel_[2], state_, samp_, acc_, dense_pos_,
         dense_vel_, offsets_, scan_status_, scan_counter_, partial_;
     DeviceBuffer t_count_, t_gpos_, t_gvel_, t_axis_, t_gate_, t_gauss_;
 };

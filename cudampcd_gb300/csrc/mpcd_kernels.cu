@@ -1,14 +1,13 @@
 // Kernels of the GB300 MPCD step.
 //
 // One launch of step_kernel completes step k of every box: for each cell it
-// stages the cell's bucket in shared memory with bulk (TMA) copies, streams the
-// particles (step k), collides them (SRD or extended MPC), undoes the grid
-// shift, accumulates the lab-grid sample if asked, streams each particle again
-// for step k+1 only to find its next cell, and scatters the post-collision
-// state into that cell's bucket of the other parity.  Particles are therefore
-// stored post-collision (the state the reference exposes between steps) and
-// keyed by their next cell; streaming is recomputed, bit-identically, where it
-// is needed.
+// stages the cell's bucket (the particles as they enter collision k: streamed
+// and shifted) in shared memory with bulk (TMA) copies, collides them (SRD or
+// extended MPC), undoes the grid shift, accumulates the lab-grid sample if
+// asked, streams each particle for step k+1 and scatters it into the bucket of
+// the cell it then occupies (the other parity).  The post-collision state the
+// reference exposes between steps is never stored: the getters recompute it by
+// replaying the last collision from its (still intact) input buckets.
 //
 // Reference path being replaced: translateParticles (simulation_kernels.cu:65-143),
 // srdCollision (srd_collision_strategy.cu:12-157), ext::fusedCollision
@@ -144,7 +143,7 @@ __device__ __forceinline__ int box_of_particle(const BoxDesc* boxes, int nboxes,
 
 // Claim a slot in `count[key]` for every active lane; lanes that share a key
 // are served by one atomic (warp-aggregated).  Returns the slot.
-__device__ __forceinline__ uint32_t claim_slot(uint32_t* count, uint64_t key, bool active)
+__device__ __forceinline__ uint32_t claim_slot(uint32_t* count, uint32_t key, bool active)
 {
     const unsigned act = __ballot_sync(kFull, active);
     uint32_t slot = 0;
@@ -160,12 +159,12 @@ __device__ __forceinline__ uint32_t claim_slot(uint32_t* count, uint64_t key, bo
 }
 
 // Accumulate (v, 1) into samp[lab] for every active lane, one atomic per distinct cell per warp.
-__device__ __forceinline__ void sample_add(float4* samp, uint64_t lab, float3 v, bool active)
+__device__ __forceinline__ void sample_add(float4* samp, uint32_t lab, float3 v, bool active)
 {
     unsigned todo = __ballot_sync(kFull, active);
     while (todo) {
         const int leader = __ffs(todo) - 1;
-        const uint64_t key = __shfl_sync(kFull, lab, leader);
+        const uint32_t key = __shfl_sync(kFull, lab, leader);
         const bool mine = active && ((todo >> (threadIdx.x & 31)) & 1u) && lab == key;
         const unsigned grp = __ballot_sync(kFull, mine);
         float sx = mine ? v.x : 0.0f, sy = mine ? v.y : 0.0f, sz = mine ? v.z : 0.0f;
@@ -180,29 +179,24 @@ __device__ __forceinline__ void sample_add(float4* samp, uint64_t lab, float3 v,
     }
 }
 
-// Write one post-collision particle into its next bucket, or into the overflow list.
-__device__ __forceinline__ void scatter_particle(const StepArgs& a, const BoxDesc& b, float3 x, float3 v,
-                                                 uint32_t id, float3 next_shift, bool active)
+// Put one particle (already streamed and shifted for the next collision, in
+// cell `key`) into its bucket, or into the overflow list when the bucket is full.
+__device__ __forceinline__ void store_particle(const StepArgs& a, const BoxDesc& b, float3 xs, float3 vs, uint32_t id,
+                                               uint32_t key, bool active)
 {
-    uint64_t key = 0;
-    if (active) {
-        float3 vn = v;
-        const float3 xn = stream_shift(b, x, vn, next_shift);
-        key = (uint64_t)b.cell_base + storage_index(b, cell_of(b, xn));
-    }
     const uint32_t slot = claim_slot(a.out_count, key, active);
     if (!active) return;
+    const float4 xp = make_float4(xs.x, xs.y, xs.z, 0.0f), vp = make_float4(vs.x, vs.y, vs.z, __uint_as_float(id));
     if (slot < b.cap) {
-        const uint64_t at = b.slot_base + (key - b.cell_base) * (uint64_t)b.cap + slot;
-        a.out_pos[at] = make_float4(x.x, x.y, x.z, 0.0f);
-        a.out_vel[at] = make_float4(v.x, v.y, v.z, __uint_as_float(id));
+        const uint64_t at = b.slot_base + (uint64_t)(key - b.cell_base) * b.cap + slot;
+        a.out_pos[at] = xp;
+        a.out_vel[at] = vp;
     } else {
         atomicAdd(&a.state->overflow_total, 1ull);
-        const unsigned parity = (unsigned)((a.step + 1) & 1);
-        const unsigned q = atomicAdd(&a.state->ov_count[parity], 1u);
+        const unsigned q = atomicAdd(&a.state->ov_count[a.ov_out_slot], 1u);
         if (q < a.ov_cap) {
-            a.ov_out_pos[q] = make_float4(x.x, x.y, x.z, 0.0f);
-            a.ov_out_vel[q] = make_float4(v.x, v.y, v.z, __uint_as_float(id));
+            a.ov_out_pos[q] = xp;
+            a.ov_out_vel[q] = vp;
         } else {
             atomicOr(&a.state->error_flags, kErrOverflowListFull);
         }
@@ -394,8 +388,9 @@ __device__ inline TileLayout carve(unsigned char* base, uint32_t pbuf, uint32_t 
     return t;
 }
 
-// Count of cell `c` of `tile` (first thread of the cell's group), zeroed as read
-// for reuse two steps later; issued one tile ahead so its latency hides.
+// Count of cell `c` of `tile` (first thread of the cell's group); issued one
+// tile ahead so its latency hides.  Outside a replay it also clears the same
+// cell of the counts of step k-1, which step k+1 will fill.
 __device__ __forceinline__ uint32_t fetch_count(const StepArgs& a, uint32_t tile, uint32_t c, bool leader)
 {
     if (!leader || tile >= a.num_tiles) return 0;
@@ -404,46 +399,48 @@ __device__ __forceinline__ uint32_t fetch_count(const StepArgs& a, uint32_t tile
     const uint32_t c0 = (tile - bp->tile_base) * bp->tile_cells;
     if (c >= min(bp->tile_cells, bp->C - c0)) return 0;
     const uint32_t g = bp->cell_base + c0 + c;
-    const uint32_t raw = a.in_count[g];
-    a.in_count[g] = 0;
-    return raw;
+    if (!a.replay) a.zero_count[g] = 0;
+    return a.in_count[g];
 }
 
 // Overflow particles of step k (they found their bucket full when step k-1
-// scattered them): as in the reference, they stream but skip the collision and
-// keep the unshifted position pbc(pbc(x + s) - s) (simulation_functions.cpp:90-93).
+// scattered them): as in the reference, they skip the collision and keep the
+// unshifted position pbc(pbc(x + s) - s) (simulation_functions.cpp:90-93).
 __device__ void overflow_pass(const StepArgs& a)
 {
-    const unsigned parity = (unsigned)(a.step & 1);
-    const uint32_t n = min(a.state->ov_count[parity], a.ov_cap);
+    const uint32_t n = min(a.state->ov_count[a.ov_in_slot], a.ov_cap);
     for (uint32_t base = 0; base < n; base += kThreads) {
         const uint32_t q = base + threadIdx.x;
         const bool active = q < n;
         int bi = 0;
-        uint32_t id = 0;
-        float3 x = make_float3(0, 0, 0), v = make_float3(0, 0, 0);
-        float3 sn = make_float3(0, 0, 0);
+        uint32_t id = 0, key = 0;
+        float3 x = make_float3(0, 0, 0), v = x, xs = x, vs = x;
         if (active) {
             const float4 p = a.ov_in_pos[q], w = a.ov_in_vel[q];
             id = __float_as_uint(w.w);
             bi = box_of_particle(a.boxes, a.nboxes, id);
             const BoxDesc& b = a.boxes[bi];
-            x = make_float3(p.x, p.y, p.z);
-            v = make_float3(w.x, w.y, w.z);
             const float3 s = grid_shift(b, bi, a.step, a.state);
-            const float3 xs = stream_shift(b, x, v, s);
-            x = pbc(b, make_float3(xs.x - s.x, xs.y - s.y, xs.z - s.z));
-            sn = grid_shift(b, bi, a.step + 1, a.state);
+            x = pbc(b, make_float3(p.x - s.x, p.y - s.y, p.z - s.z));   // post-step state
+            v = make_float3(w.x, w.y, w.z);
+            if (a.replay) {
+                const uint64_t i3 = 3 * (uint64_t)id;
+                a.dense_pos[i3] = x.x; a.dense_pos[i3 + 1] = x.y; a.dense_pos[i3 + 2] = x.z;
+                a.dense_vel[i3] = v.x; a.dense_vel[i3 + 1] = v.y; a.dense_vel[i3 + 2] = v.z;
+            } else {
+                vs = v;
+                xs = stream_shift(b, x, vs, grid_shift(b, bi, a.step + 1, a.state));
+                key = b.cell_base + storage_index(b, cell_of(b, xs));
+            }
         }
+        if (a.replay) continue;
         const BoxDesc& b = a.boxes[bi];
         if (a.sample) {
-            const uint64_t lab = active ? (uint64_t)b.cell_base + ref_index(b, cell_of(b, x)) : 0;
+            const uint32_t lab = active ? b.cell_base + ref_index(b, cell_of(b, x)) : 0;
             sample_add(a.samp, lab, v, active);
         }
-        scatter_particle(a, b, x, v, id, sn, active);
+        store_particle(a, b, xs, vs, id, key, active);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) a.state->ov_count[parity] = 0;
 }
 
 // Sum over the G lanes of a cell group (G a power of two dividing 32).
@@ -454,7 +451,7 @@ __device__ __forceinline__ T group_sum(T v, uint32_t G)
     return v;
 }
 
-template <int ALGO, bool TABLE, bool SINGLE>
+template <int ALGO, bool TABLE, bool SINGLE, bool REPLAY>
 __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32_t pbuf)
 {
     using D = Draws<TABLE>;
@@ -482,7 +479,10 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
     __syncthreads();
     uint32_t phase = 0;
 
-    if (blockIdx.x == 0) overflow_pass(a);
+    if (blockIdx.x == 0) {
+        if (tid == 0 && !a.replay) a.state->ov_count[a.ov_zero_slot] = 0;   // list of step k-1, refilled by step k+1
+        overflow_pass(a);
+    }
 
     // group of G threads per cell (every box of a launch has the same tile size)
     const uint32_t G = kThreads / tcells;
@@ -630,28 +630,22 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                 __syncthreads();
             }
 
-            // stream step k (recomputed); extended: rank by particle id
-            for (uint32_t p = tid; p < np; p += kThreads) {
-                const uint32_t ci = s_cell[p];
-                const uint32_t o = L.off[ci] - pbase;
-                const uint32_t r = p - o;
-                const uint32_t n = L.cnt[ci];
-                if (r < n) {
-                    const float4 xp = s_pos[p], vp = s_vel[p];
-                    float3 x = make_float3(xp.x, xp.y, xp.z), v = make_float3(vp.x, vp.y, vp.z);
-                    x = stream_shift(b, x, v, s);
-                    s_pos[p] = make_float4(x.x, x.y, x.z, xp.w);
-                    s_vel[p] = make_float4(v.x, v.y, v.z, vp.w);
-                    if (ALGO == 1) {
-                        const uint32_t id = __float_as_uint(vp.w);
+            // extended: rank of every real particle within its cell by particle id
+            if (ALGO == 1) {
+                for (uint32_t p = tid; p < np; p += kThreads) {
+                    const uint32_t ci = s_cell[p];
+                    const uint32_t o = L.off[ci] - pbase;
+                    const uint32_t n = L.cnt[ci];
+                    if (p - o < n) {
+                        const uint32_t id = __float_as_uint(s_vel[p].w);
                         uint32_t rank = 0;
                         for (uint32_t q = 0; q < n; ++q) rank += __float_as_uint(s_vel[o + q].w) < id;
                         s_rank[p] = (uint16_t)rank;
                         s_inv[o + rank] = (uint16_t)p;
                     }
                 }
+                __syncthreads();
             }
-            __syncthreads();
 
             // per-cell collision quantities, one group per cell
             if (ALGO == 0) {
@@ -819,20 +813,30 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                             x = pbc(b, make_float3((com.x + x.x) - s.x, (com.y + x.y) - s.y, (com.z + x.z) - s.z));
                         }
                     }
-                    float3 vn = v;
-                    const float3 xn = stream_shift(b, x, vn, sn);
-                    s_key[p] = b.cell_base + storage_index(b, cell_of(b, xn));
-                    s_pos[p] = make_float4(x.x, x.y, x.z, 0.0f);
-                    s_vel[p] = make_float4(v.x, v.y, v.z, vp.w);
+                    if (REPLAY) {
+                        const uint64_t i3 = 3 * (uint64_t)__float_as_uint(vp.w);
+                        a.dense_pos[i3] = x.x; a.dense_pos[i3 + 1] = x.y; a.dense_pos[i3 + 2] = x.z;
+                        a.dense_vel[i3] = v.x; a.dense_vel[i3 + 1] = v.y; a.dense_vel[i3 + 2] = v.z;
+                    } else {
+                        float3 vn = v;
+                        const float3 xn = stream_shift(b, x, vn, sn);
+                        s_key[p] = b.cell_base + storage_index(b, cell_of(b, xn));
+                        s_pos[p] = make_float4(xn.x, xn.y, xn.z, 0.0f);
+                        s_vel[p] = make_float4(vn.x, vn.y, vn.z, vp.w);
+                    }
                 } else if (p < np) {
                     s_key[p] = kNoKey;
                 }
-                if (a.sample) {
-                    const uint64_t lab = active ? (uint64_t)b.cell_base + ref_index(b, cell_of(b, x)) : 0;
+                if (!REPLAY && a.sample) {
+                    const uint32_t lab = active ? b.cell_base + ref_index(b, cell_of(b, x)) : 0;
                     sample_add(a.samp, lab, v, active);
                 }
             }
             __syncthreads();
+            if (REPLAY) {
+                i0 = i1;
+                continue;
+            }
 
             // claim bucket slots (warp-aggregated atomics, all issued before any
             // result is used), then write the particles to their buckets
@@ -864,8 +868,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                         a.out_vel[at] = vp;
                     } else {
                         atomicAdd(&a.state->overflow_total, 1ull);
-                        const unsigned parity = (unsigned)((a.step + 1) & 1);
-                        const unsigned q = atomicAdd(&a.state->ov_count[parity], 1u);
+                        const unsigned q = atomicAdd(&a.state->ov_count[a.ov_out_slot], 1u);
                         if (q < a.ov_cap) {
                             a.ov_out_pos[q] = xp;
                             a.ov_out_vel[q] = vp;
@@ -883,9 +886,9 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
 
 // ------------------------------------------------------------------ prologue scatter
 
-// Key dense clean particles by their cell after streaming step k and scatter them
-// into the buckets of parity k; particle id = prev = dense index.  The launch
-// plays the epilogue of step k-1: a.step = k - 1, a.out_* = buckets of parity k.
+// Stream dense post-step particles for step k (a.step = k - 1: the launch plays
+// the epilogue of step k-1), key them by the cell they then occupy and scatter
+// them into the buckets of step k (a.out_*); particle id = dense index.
 __global__ void __launch_bounds__(kThreads) scatter_kernel(StepArgs a, const float* pos, const float* vel,
                                                            uint64_t n_total)
 {
@@ -893,15 +896,17 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(StepArgs a, const flo
         const uint64_t i = base + threadIdx.x;
         const bool active = i < n_total;
         int bi = 0;
-        float3 x = make_float3(0, 0, 0), v = make_float3(0, 0, 0);
-        float3 s = make_float3(0, 0, 0);
+        uint32_t key = 0;
+        float3 xs = make_float3(0, 0, 0), vs = xs;
         if (active) {
             bi = box_of_particle(a.boxes, a.nboxes, i);
-            x = make_float3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
-            v = make_float3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
-            s = grid_shift(a.boxes[bi], bi, a.step + 1, a.state);
+            const BoxDesc& b = a.boxes[bi];
+            vs = make_float3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+            xs = stream_shift(b, make_float3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), vs,
+                              grid_shift(b, bi, a.step + 1, a.state));
+            key = b.cell_base + storage_index(b, cell_of(b, xs));
         }
-        scatter_particle(a, a.boxes[bi], x, v, (uint32_t)i, s, active);
+        store_particle(a, a.boxes[bi], xs, vs, (uint32_t)i, key, active);
     }
 }
 
@@ -1056,65 +1061,16 @@ __global__ void compact_overflow_kernel(const BoxDesc* boxes, int nboxes, uint64
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         const uint64_t d = (uint64_t)base + q;
         if (d >= n_total) break;
-        if (out_cell) {   // the cell the particle was keyed to (streamed with the shift of step `step`)
+        if (out_cell) {   // the cell the (already streamed) particle is keyed to
             const float4 p = ov_pos[q], w = ov_vel[q];
             const int bi = box_of_particle(boxes, nboxes, __float_as_uint(w.w));
             const BoxDesc& b = boxes[bi];
-            float3 v = make_float3(w.x, w.y, w.z);
-            const float3 xs = stream_shift(b, make_float3(p.x, p.y, p.z), v, grid_shift(b, bi, step, st));
-            out_cell[d] = b.cell_base + ref_index(b, cell_of(b, xs));
+            out_cell[d] = b.cell_base + ref_index(b, cell_of(b, make_float3(p.x, p.y, p.z)));
         }
         if (out_slot) out_slot[d] = (uint32_t)(total_slots + q);
         if (out_prev) out_prev[d] = __float_as_uint(ov_vel[q].w);
         if (out_id) out_id[d] = __float_as_uint(ov_vel[q].w);
     }
-}
-
-// Getter: every stored particle to its id in dense (N, 3) arrays.
-__global__ void __launch_bounds__(kThreads) gather_kernel(const StepArgs a, const uint32_t* count, const float4* pos,
-                                                          const float4* vel, uint64_t cells, uint64_t n_total,
-                                                          const float4* ov_pos,
-                                                          const float4* ov_vel, unsigned parity, float* out_pos,
-                                                          float* out_vel, unsigned int* n_seen)
-{
-    uint32_t seen = 0;
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells;
-         c += (uint64_t)gridDim.x * blockDim.x) {
-        int lo = 0, hi = a.nboxes - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (a.boxes[mid].cell_base <= c) lo = mid; else hi = mid - 1;
-        }
-        const BoxDesc& b = a.boxes[lo];
-        const uint32_t n = min(count[c], b.cap);
-        const uint64_t slot0 = b.slot_base + (c - b.cell_base) * b.cap;
-        for (uint32_t q = 0; q < n; ++q) {
-            const float4 x = pos[slot0 + q], w = vel[slot0 + q];
-            const uint64_t id = __float_as_uint(w.w);
-            if (id >= n_total) {
-                atomicOr(&a.state->error_flags, kErrKeyMismatch);
-                continue;
-            }
-            if (out_pos) { out_pos[3 * id] = x.x; out_pos[3 * id + 1] = x.y; out_pos[3 * id + 2] = x.z; }
-            if (out_vel) { out_vel[3 * id] = w.x; out_vel[3 * id + 1] = w.y; out_vel[3 * id + 2] = w.z; }
-        }
-        seen += n;
-    }
-    if (blockIdx.x == 0) {
-        const uint32_t m = min(a.state->ov_count[parity], a.ov_cap);
-        for (uint32_t q = threadIdx.x; q < m; q += blockDim.x) {
-            const float4 x = ov_pos[q], w = ov_vel[q];
-            const uint64_t id = __float_as_uint(w.w);
-            if (id >= n_total) {
-                atomicOr(&a.state->error_flags, kErrKeyMismatch);
-                continue;
-            }
-            if (out_pos) { out_pos[3 * id] = x.x; out_pos[3 * id + 1] = x.y; out_pos[3 * id + 2] = x.z; }
-            if (out_vel) { out_vel[3 * id] = w.x; out_vel[3 * id + 1] = w.y; out_vel[3 * id + 2] = w.z; }
-        }
-        if (threadIdx.x == 0) seen += m;
-    }
-    atomicAdd(n_seen, seen);
 }
 
 // ------------------------------------------------------------------ initialisation
@@ -1189,15 +1145,23 @@ size_t step_smem_bytes(uint32_t pbuf, uint32_t cells, int algorithm) { return ti
 
 namespace {
 using StepFn = void (*)(const StepArgs, uint32_t);
-constexpr StepFn kStepFns[2][2][2] = {
-    {{step_kernel<0, false, false>, step_kernel<0, false, true>}, {step_kernel<0, true, false>, step_kernel<0, true, true>}},
-    {{step_kernel<1, false, false>, step_kernel<1, false, true>}, {step_kernel<1, true, false>, step_kernel<1, true, true>}}};
+// [algorithm][table draws][single box][replay]
+const StepFn kStepFns[2][2][2][2] = {
+    {{{step_kernel<0, false, false, false>, step_kernel<0, false, false, true>},
+      {step_kernel<0, false, true, false>, step_kernel<0, false, true, true>}},
+     {{step_kernel<0, true, false, false>, step_kernel<0, true, false, true>},
+      {step_kernel<0, true, true, false>, step_kernel<0, true, true, true>}}},
+    {{{step_kernel<1, false, false, false>, step_kernel<1, false, false, true>},
+      {step_kernel<1, false, true, false>, step_kernel<1, false, true, true>}},
+     {{step_kernel<1, true, false, false>, step_kernel<1, true, false, true>},
+      {step_kernel<1, true, true, false>, step_kernel<1, true, true, true>}}}};
 }  // namespace
 
 cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st)
 {
     const size_t smem = step_smem_bytes(pbuf, a.boxes_tile_cells, algorithm);
-    kStepFns[algorithm ? 1 : 0][table ? 1 : 0][a.nboxes == 1 ? 1 : 0]<<<grid, kThreads, smem, st>>>(a, pbuf);
+    kStepFns[algorithm ? 1 : 0][table ? 1 : 0][a.nboxes == 1 ? 1 : 0][a.replay ? 1 : 0]<<<grid, kThreads, smem, st>>>(
+        a, pbuf);
     return cudaGetLastError();
 }
 
@@ -1206,13 +1170,14 @@ cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* bl
     const size_t smem = step_smem_bytes(pbuf, cells, algorithm);
     for (int i = 0; i < 2; ++i)
         for (int j = 0; j < 2; ++j)
-            for (int k = 0; k < 2; ++k) {
-                cudaError_t e = cudaFuncSetAttribute((const void*)kStepFns[i][j][k],
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                if (e != cudaSuccess) return e;
-            }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, (const void*)kStepFns[algorithm ? 1 : 0][0][1],
-                                                         kThreads, smem);
+            for (int k = 0; k < 2; ++k)
+                for (int r = 0; r < 2; ++r) {
+                    cudaError_t e = cudaFuncSetAttribute((const void*)kStepFns[i][j][k][r],
+                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                    if (e != cudaSuccess) return e;
+                }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        blocks_per_sm, (const void*)kStepFns[algorithm ? 1 : 0][0][1][0], kThreads, smem);
 }
 
 cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel, uint64_t n_total, int grid,
@@ -1247,15 +1212,6 @@ cudaError_t launch_layout(const StepArgs& a, const uint32_t* count, const float4
     compact_overflow_kernel<<<8, kThreads, 0, st>>>(a.boxes, a.nboxes, a.step, ov_pos, ov_vel, a.state, parity,
                                                     a.ov_cap, offsets, cells, n_total, a.total_slots, out_cell,
                                                     out_slot, out_prev, out_id);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_gather(const StepArgs& a, const uint32_t* count, const float4* pos, const float4* vel,
-                          uint64_t cells, uint64_t n_total, const float4* ov_pos, const float4* ov_vel, unsigned parity,
-                          float* out_pos, float* out_vel, unsigned int* n_seen, int grid, cudaStream_t st)
-{
-    gather_kernel<<<grid, kThreads, 0, st>>>(a, count, pos, vel, cells, n_total, ov_pos, ov_vel, parity, out_pos,
-                                             out_vel, n_seen);
     return cudaGetLastError();
 }
 

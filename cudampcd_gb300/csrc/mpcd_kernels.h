@@ -30,10 +30,6 @@ cudaError_t launch_layout(const StepArgs& a, const uint32_t* count, const float4
                           unsigned int* tile_counter, const float4* ov_pos, const float4* ov_vel, unsigned parity,
                           uint32_t* out_cell, uint32_t* out_slot, uint32_t* out_prev, uint32_t* out_id, int grid,
                           cudaStream_t st);
-// Getter: every stored particle to its id in (N, 3) arrays; n_seen += particles written.
-cudaError_t launch_gather(const StepArgs& a, const uint32_t* count, const float4* pos, const float4* vel,
-                          uint64_t cells, uint64_t n_total, const float4* ov_pos, const float4* ov_vel, unsigned parity,
-                          float* out_pos, float* out_vel, unsigned int* n_seen, int grid, cudaStream_t st);
 size_t scan_status_words(uint64_t cells);
 // Initial particles (uniform positions, Maxwell-Boltzmann velocities).
 cudaError_t launch_init(const BoxDesc* boxes, int nboxes, float* pos, float* vel, uint64_t n_total, int grid,

@@ -2,11 +2,15 @@
 //
 // Particles live in per-cell buckets: cell c of a box owns `cap` slots
 // (cap = 4n, the depth of the reference's cell table, backend_context.cu:24),
-// stored as two float4 arrays: pos = (x, y, z, prev) and vel = (vx, vy, vz, 0),
-// where `prev` is the particle's position in the previous layout (its stable
-// sort key).  Cells are numbered in storage order, z fastest, then x, then y,
-// so that the up to 27 source cells of any destination cell are processed
-// within a short window of the sweep.  Two bucket sets alternate by step parity.
+// stored as two float4 arrays: pos = (x, y, z, 0) and vel = (vx, vy, vz, id).
+// A bucket set for step k holds every particle as it enters the collision of
+// step k: streamed and shifted by the grid shift of step k, in the bucket of the
+// cell it then occupies (the reference's translate output, simulation_functions.cpp:38-103).
+// Cells are numbered in storage order, z fastest, then x, then y, so that the
+// up to 27 source cells of any destination cell are processed within a short
+// window of the sweep.  Two bucket sets alternate by step parity; the cell
+// counts rotate over three arrays so that the inputs of the last step survive
+// it (the getters replay that step's collision from them).
 #pragma once
 
 #include <cstdint>
@@ -38,6 +42,7 @@ struct BoxDesc {
     uint32_t tile_cells;   // cells per tile
     uint64_t slot_base;    // first global slot of this box
     uint64_t dense_base;   // first particle of this box in dense (getter) arrays
+    uint64_t div_z, div_x; // ceil(2^48 / Lz), ceil(2^48 / Lx): exact division of cell indices < 2^31
     uint32_t seed_lo, seed_hi;
 };
 
@@ -50,8 +55,7 @@ struct alignas(32) SampleAcc {
 struct DeviceState {
     unsigned long long overflow_total;   // particles that found their bucket full
     unsigned int error_flags;            // kErr* bits
-    unsigned int ov_count[2];            // overflow list fill, by step parity
-    unsigned int pad;
+    unsigned int ov_count[3];            // overflow list fill, by step modulo 3
     // injected grid shifts (test hook), valid when inject_valid[i] != 0
     unsigned long long inject_step[kMaxInjectedShifts];
     float inject_shift[kMaxInjectedShifts][4];
@@ -83,20 +87,27 @@ struct StepArgs {
     uint32_t num_tiles;
     uint64_t total_slots;
     uint64_t step;                // k: this launch completes step k
-    // buckets holding clean(k), keyed by the cell after streaming step k
+    // buckets holding the particles entering collision k (streamed, shifted)
     const float4* in_pos;
     const float4* in_vel;
-    uint32_t* in_count;           // zeroed as read
-    // buckets receiving clean(k+1), keyed by the cell after streaming step k+1
+    const uint32_t* in_count;
+    // buckets receiving the particles entering collision k+1
     float4* out_pos;
     float4* out_vel;
     uint32_t* out_count;
+    uint32_t* zero_count;         // counts of step k-1: cleared here for step k+1
     // overflow lists: in = pending for step k, out = for step k+1
     const float4* ov_in_pos;
     const float4* ov_in_vel;
     float4* ov_out_pos;
     float4* ov_out_vel;
     uint32_t ov_cap;
+    uint32_t ov_in_slot, ov_out_slot, ov_zero_slot;   // indices into DeviceState::ov_count
+    // replay: recompute collision k and write the post-collision state to dense
+    // (N, 3) arrays by particle id, changing nothing else
+    int32_t replay;
+    float* dense_pos;
+    float* dense_vel;
     DeviceState* state;
     int32_t sample;               // accumulate the lab-grid sample of clean(k+1)
     float4* samp;                 // [global cells] (sum vx, vy, vz, count)
