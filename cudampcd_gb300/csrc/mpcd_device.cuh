@@ -68,17 +68,15 @@ __device__ __forceinline__ float3 grid_shift(const BoxDesc& b, int box_index, ui
 // ------------------------------------------------------------------ geometry
 
 // apply_periodic_boundaries of the reference: fmodf(r + 1.5 L, L) - 0.5 L.
-// For r + 1.5L in [0, 3L) the remainder is a - qL with q in {0,1,2}, and that
-// difference is exact (Sterbenz), i.e. identical to fmodf; other arguments
-// take fmodf itself.
+// For a = r + 1.5L in [0, 3L) the remainder is a - qL with q in {0,1,2}, and
+// that difference is exact (Sterbenz), i.e. identical to fmodf.  The common
+// case is evaluated branch-free; arguments outside [0, 3L) take fmodf itself.
 __device__ __forceinline__ float pbc1(float r, float L)
 {
     const float a = r + 1.5f * L;
-    float m;
-    if (a >= 0.0f && a < 3.0f * L)
-        m = a >= 2.0f * L ? a - 2.0f * L : (a >= L ? a - L : a);
-    else
-        m = fmodf(a, L);
+    const float q = a >= 2.0f * L ? 2.0f * L : (a >= L ? L : 0.0f);
+    float m = a - q;
+    if (__builtin_expect(!(a >= 0.0f && a < 3.0f * L), 0)) m = fmodf(a, L);
     return m - L * 0.5f;
 }
 
@@ -92,11 +90,10 @@ __device__ __forceinline__ float3 pbc(const BoxDesc& b, float3 r)
 __device__ __forceinline__ uint32_t cell_coord(float x, float Lf, uint32_t L)
 {
     const float f = floorf(x + Lf * 0.5f);
-    if (f >= 0.0f && f < Lf)
-        return (uint32_t)f;
-    if (f == Lf)
-        return 0u;
-    return (uint32_t)(long long)f % L;
+    uint32_t c = (uint32_t)(int)f;
+    c = c == L ? 0u : c;
+    if (__builtin_expect(!(f >= 0.0f && f <= Lf), 0)) c = (uint32_t)(long long)f % L;
+    return c;
 }
 
 __device__ __forceinline__ uint3 cell_of(const BoxDesc& b, float3 x)

@@ -60,13 +60,28 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return ok != 0;
 }
 
+// As mbar_try_wait, but the thread may sleep up to `ns` nanoseconds in the
+// barrier instead of spinning.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t ns)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+        : "memory");
+    return ok != 0;
+}
+
 // Wait for the phase with the given parity; false after kWaitLimitNs.
 __device__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
 {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait_sleep(bar, parity, 1000000u)) return true;
     const uint64_t t0 = globaltimer();
     while (true) {
-        if (mbar_try_wait(bar, parity)) return true;
+        if (mbar_try_wait_sleep(bar, parity, 1000000u)) return true;
         if (globaltimer() - t0 > kWaitLimitNs) return false;
     }
 }
@@ -543,17 +558,16 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
             }
         }
         next_raw = fetch_count(a, tile + gridDim.x, my_cell, leader);
-        uint32_t total;
-        const uint32_t off = block_exclusive_scan(mine + mine_g, warp_tot, total);
-        uint32_t gtotal;
-        const uint32_t goff = block_exclusive_scan(mine_g, warp_tot, gtotal);
+        // one scan of (particles << 16 | ghosts): a tile holds fewer than 2^16 of either
+        uint32_t packed_total;
+        const uint32_t packed = block_exclusive_scan(((mine + mine_g) << 16) | mine_g, warp_tot, packed_total);
         if (leader && my_cell < nc) {
-            L.off[my_cell] = off;
-            L.goff[my_cell] = goff;
+            L.off[my_cell] = packed >> 16;
+            L.goff[my_cell] = packed & 0xFFFFu;
         }
         if (tid == 0) {
-            L.off[nc] = total;
-            L.goff[nc] = gtotal;
+            L.off[nc] = packed_total >> 16;
+            L.goff[nc] = packed_total & 0xFFFFu;
         }
         __syncthreads();
 
@@ -561,6 +575,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
         uint32_t i0 = 0;
         while (i0 < nc) {
             uint32_t lo = i0 + 1, hi = nc;   // largest i1 with off[i1] - off[i0] <= pbuf
+            if (L.off[nc] - L.off[i0] <= pbuf) lo = nc;   // the common case: the rest fits
             while (lo < hi) {
                 const uint32_t mid = (lo + hi + 1) >> 1;
                 if (L.off[mid] - L.off[i0] <= pbuf) lo = mid; else hi = mid - 1;
