@@ -70,6 +70,7 @@ def lib() -> C.CDLL:
         L.mpcd_gb_dump_layout.argtypes = [H, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.mpcd_gb_inject_draws.argtypes = [H, C.c_uint32, C.c_uint32] + [C.c_void_p] * 6
         L.mpcd_gb_counters.argtypes = [H, u64p]
+        L.mpcd_gb_cell_offsets_noalloc.argtypes = [H, C.c_void_p, C.c_uint64]
         _lib = L
     return _lib
 
@@ -183,6 +184,11 @@ class Handle:
         out = np.zeros(2, np.uint64)
         self._check(self._lib.mpcd_gb_counters(self.h, out))
         return int(out[0]), int(out[1])
+
+    def cell_offsets_noalloc(self, d_offsets: int, n_offsets: int):
+        """Queue the cell offsets of the current layout into the device buffer at
+        address d_offsets (n_offsets uint32 entries) on the handle's stream."""
+        self._check(self._lib.mpcd_gb_cell_offsets_noalloc(self.h, C.c_void_p(d_offsets), n_offsets))
 
     def set_stream(self, stream_ptr):
         self._check(self._lib.mpcd_gb_set_stream(self.h, C.c_void_p(stream_ptr)))

@@ -219,6 +219,28 @@ public:
         check(cudaStreamSynchronize(stream_), "dump");
     }
 
+    // Cell offsets of the current layout into a caller's device buffer; the
+    // scan's scratch is the library's static per-device array, nothing is allocated.
+    void cell_offsets_noalloc(uint32_t* d_offsets, uint64_t n_offsets)
+    {
+        char msg[160];
+        if (cells_ > MPCD_GB_NOALLOC_MAX_CELLS) {
+            std::snprintf(msg, sizeof msg, "cell offsets: %llu cells exceed the limit of %llu of the static scan scratch",
+                          (unsigned long long)cells_, (unsigned long long)MPCD_GB_NOALLOC_MAX_CELLS);
+            throw Error(MPCD_GB_EINVAL, msg);
+        }
+        if (!d_offsets) throw Error(MPCD_GB_EINVAL, "cell offsets: null output buffer");
+        if (n_offsets < cells_ + 1) {
+            std::snprintf(msg, sizeof msg, "cell offsets: buffer of %llu entries, %llu needed",
+                          (unsigned long long)n_offsets, (unsigned long long)(cells_ + 1));
+            throw Error(MPCD_GB_EINVAL, msg);
+        }
+        StepArgs a = args(step_);
+        check(launch_cell_offsets_static(a, count_[step_ % 3].as<uint32_t>(), cells_, d_offsets,
+                                         (int)params_.device_id, stream_),
+              "cell offsets");
+    }
+
     // The overflow list is filled in arrival order; order its part of a dump by
     // (cell, id) so that a dump is deterministic.
     void sort_overflow_tail(uint32_t* cell, uint32_t* slot, uint32_t* id)
@@ -842,6 +864,11 @@ int32_t mpcd_gb_counters(mpcd_gb_handle* h, uint64_t out[2])
 {
     if (!out) return MPCD_GB_EINVAL;
     return guarded(h, [&](mpcd_gb::Engine& e) { e.counters(out); });
+}
+
+int32_t mpcd_gb_cell_offsets_noalloc(mpcd_gb_handle* h, uint32_t* d_offsets, uint64_t n_offsets)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.cell_offsets_noalloc(d_offsets, n_offsets); });
 }
 
 }  // extern "C"

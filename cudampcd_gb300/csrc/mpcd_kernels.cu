@@ -15,9 +15,11 @@
 // and the sampling kernels (simulation_kernels.cu:150-230); the arithmetic
 // follows the CPU backend (cpu_backend/simulation_functions.cpp:38-406).
 #include <cstdio>
+#include <mutex>
 
 #include "mpcd_device.cuh"
 #include "mpcd_kernels.h"
+#include "mpcd_gb.h"
 
 namespace mpcd_gb {
 
@@ -1252,5 +1254,62 @@ cudaError_t launch_subtract(float* vel, uint64_t begin, uint64_t end, float mx, 
 }
 
 size_t scan_status_words(uint64_t cells) { return (cells + kThreads * kScanItems - 1) / (kThreads * kScanItems); }
+
+// ------------------------------------------------------------------ allocation-free cell offsets
+//
+// scan_kernel with its scratch in a fixed file-scope array instead of buffers
+// allocated by the caller: kStaticScanTiles look-back status words followed by
+// the tile counter (one 64-bit word).  16384 tiles of 2048 cells = 33,554,432
+// cells; 128 KiB of device memory per device, allocated with the module.
+constexpr uint64_t kStaticScanTiles = 16384;
+constexpr int kMaxScratchDevices = 64;
+static_assert(kStaticScanTiles * kThreads * kScanItems == MPCD_GB_NOALLOC_MAX_CELLS,
+              "static scan scratch and the ABI limit disagree");
+
+static __device__ __align__(256) unsigned long long g_static_scan_scratch[kStaticScanTiles + 1];
+
+// Address of this device's scratch: looked up once per device, with that device current.
+static cudaError_t static_scan_scratch(int device, unsigned long long** out)
+{
+    static std::mutex mu;
+    static unsigned long long* address[kMaxScratchDevices] = {};
+    if (device < 0 || device >= kMaxScratchDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!address[device]) {
+        int current = -1;
+        cudaError_t e = cudaGetDevice(&current);
+        if (e != cudaSuccess) return e;
+        if (current != device && (e = cudaSetDevice(device)) != cudaSuccess) return e;
+        unsigned long long* ptr = nullptr;
+        e = cudaGetSymbolAddress((void**)&ptr, g_static_scan_scratch);
+        if (current != device) {
+            const cudaError_t r = cudaSetDevice(current);
+            if (e == cudaSuccess) e = r;
+        }
+        if (e != cudaSuccess) return e;
+        address[device] = ptr;
+    }
+    *out = address[device];
+    return cudaSuccess;
+}
+
+cudaError_t launch_cell_offsets_static(const StepArgs& a, const uint32_t* count, uint64_t cells, uint32_t* offsets,
+                                       int device, cudaStream_t st)
+{
+    if (cells == 0 || cells > MPCD_GB_NOALLOC_MAX_CELLS) return cudaErrorInvalidValue;
+    unsigned long long* scratch = nullptr;
+    cudaError_t e = static_scan_scratch(device, &scratch);
+    if (e != cudaSuccess) return e;
+    const uint64_t tiles = (cells + kThreads * kScanItems - 1) / (kThreads * kScanItems);
+    // the status words of the tiles in use and the tile counter start at zero
+    e = cudaMemsetAsync(scratch, 0, sizeof(unsigned long long) * tiles, st);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(scratch + kStaticScanTiles, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    scan_kernel<<<(unsigned)tiles, kThreads, 0, st>>>(count, a.boxes, a.nboxes, cells, offsets, scratch,
+                                                      reinterpret_cast<unsigned int*>(scratch + kStaticScanTiles),
+                                                      a.state);
+    return cudaGetLastError();
+}
 
 }  // namespace mpcd_gb

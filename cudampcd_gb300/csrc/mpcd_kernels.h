@@ -31,6 +31,10 @@ cudaError_t launch_layout(const StepArgs& a, const uint32_t* count, const float4
                           uint32_t* out_cell, uint32_t* out_slot, uint32_t* out_prev, uint32_t* out_id, int grid,
                           cudaStream_t st);
 size_t scan_status_words(uint64_t cells);
+// Exclusive scan of min(count, cap) into offsets (cells + 1 entries), its scratch
+// in a static per-device array: allocates nothing.  cells <= MPCD_GB_NOALLOC_MAX_CELLS.
+cudaError_t launch_cell_offsets_static(const StepArgs& a, const uint32_t* count, uint64_t cells, uint32_t* offsets,
+                                       int device, cudaStream_t st);
 // Initial particles (uniform positions, Maxwell-Boltzmann velocities).
 cudaError_t launch_init(const BoxDesc* boxes, int nboxes, float* pos, float* vel, uint64_t n_total, int grid,
                         cudaStream_t st);

@@ -150,6 +150,49 @@ int32_t mpcd_gb_inject_draws(mpcd_gb_handle *h, uint32_t gmax, uint32_t pmax, co
  * [1] error flags (bit 0 overflow list full, bit 1 wait timeout, bit 2 key mismatch). */
 int32_t mpcd_gb_counters(mpcd_gb_handle *h, uint64_t out[2]);
 
+/* ---- allocation-free cell offsets (no counterpart in the reference) ---- */
+
+/* Largest cell count (C) that mpcd_gb_cell_offsets_noalloc accepts. */
+#define MPCD_GB_NOALLOC_MAX_CELLS 33554432u
+
+/* Where each cell's particles begin in the current layout, written to device memory
+ * without allocating anything on the device.
+ *
+ * d_offsets: device buffer of n_offsets >= C + 1 uint32 entries.  d_offsets[s] is the
+ * number of bucketed particles in the cells before cell s, cells in storage order
+ * (z fastest, then x, then y), i.e. the index at which cell s's run starts in the
+ * mpcd_gb_dump_layout order; d_offsets[C] is the number of bucketed particles
+ * (particles in the cell overflow list, if any, are not counted).
+ *
+ * Who needs it: a caller that cannot allocate device memory while it runs.  A coupled
+ * code (a solute or MD solver stepping with the fluid) that has handed all free HBM to
+ * its own memory pool, or a per-step loop that must not stall on cudaFree (which
+ * synchronises the whole device), can still read the cell layout every step.
+ * mpcd_gb_dump_layout allocates device buffers per call and cannot serve them.
+ *
+ * Scratch: the prefix scan's look-back status words and its tile counter live in one
+ * fixed 128 KiB array in the library's device memory, one per device.  No device memory
+ * is allocated or freed; on success no host memory either (an error message may).
+ * Limit: C <= MPCD_GB_NOALLOC_MAX_CELLS (16384 scan tiles of 2048 cells).  A larger C,
+ * a NULL d_offsets or n_offsets < C + 1 returns MPCD_GB_EINVAL before any work.
+ * What must start at zero: the status words of the tiles in use and the tile counter.
+ * Every call zeroes them on the handle's stream before its scan, so nothing needs to be
+ * cleared by the caller.
+ *
+ * Set-up: the first call on a device, with that device made current for the look-up,
+ * finds the scratch address with cudaGetSymbolAddress, which may load the library's
+ * device code.  If the calling stream is going to be captured, make that first call
+ * before the capture begins.
+ *
+ * Concurrency: the work is queued on the handle's stream (mpcd_gb_set_stream) and the
+ * call returns without waiting; order reads of d_offsets after that stream.  All calls
+ * on one device share the one scratch array, so two calls that overlap in time race and
+ * both results are undefined: calls queued on one stream are ordered and safe, calls on
+ * different streams, handles or host threads of one device must be serialised by the
+ * caller.  A look-back wait that times out sets error bit 1 (mpcd_gb_counters), which
+ * the next mpcd_gb_step, mpcd_gb_step_and_sample or setter reports as MPCD_GB_EDEVICE. */
+int32_t mpcd_gb_cell_offsets_noalloc(mpcd_gb_handle *h, uint32_t *d_offsets, uint64_t n_offsets);
+
 #ifdef __cplusplus
 }
 #endif
