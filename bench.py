@@ -8,6 +8,10 @@ benchmark (benchmark.py:36-47).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
+Profiling options (the default run uses none of them): --size LX LY LZ replaces
+the fluid cells of the workload (walls are added in z), --algorithm extended
+switches the collision, --no-e2e and --no-cpu skip those parts.
+
 One JSON line on rank 0.  `value` is device-timed particle-steps/s with the
 state resident in HBM; `e2e` is the same metric through the Python API the
 reference exposes (Simulation.step_and_sample + get_mean_fields, host wall
@@ -172,6 +176,44 @@ def run_reference_arm(args, rank):
 
 # ---------------------------------------------------------------- GPU arm
 
+def run_e2e(args, wl, algorithm, rank, local_rank, dist, world, N):
+    """Same metric through the Python API the reference exposes: a fresh
+    Simulation, step_and_sample over the timed steps and get_mean_fields (the
+    device-to-host read of the result), host wall clock."""
+    import torch
+
+    import cudampcd_gb300 as pympcd
+
+    params = pympcd.Params()
+    params.n = wl["n"]
+    params.temperature = wl["temperature"]
+    params.volume_size = (wl["L"][0], wl["L"][1], wl["L"][2] - 2)
+    params.periodicity = wl["periodic"]
+    params.drag = wl["drag"]
+    params.delta_t = wl["dt"]
+    params.algorithm = "extended" if algorithm else "srd"
+    params.device_id = local_rank
+    params.seed = wl["seed"] + rank
+    sim = pympcd.Simulation(params, "cuda")
+    sim.step_and_sample(min(args.warmup, 5))
+    sim.get_mean_fields()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    sim.step_and_sample(args.steps)
+    density, velocity = sim.get_mean_fields()
+    e2e_s = time.perf_counter() - t0
+    del sim
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * N * args.steps / e2e_s
+    d2h = (density.nbytes + velocity.nbytes) / args.steps
+    return {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,
+            "api": "cudampcd_gb300.Simulation.step_and_sample + get_mean_fields (host wall clock)"}
+
+
 def run_gpu_arm(args, rank, world, local_rank):
     import torch
 
@@ -185,8 +227,16 @@ def run_gpu_arm(args, rank, world, local_rank):
         dist.init_process_group("nccl")
 
     wl = dict(WORKLOAD)
+    workload_name = WORKLOAD_NAME
+    algorithm = 1 if args.algorithm == "extended" else 0
+    if args.size or algorithm:
+        if args.size:
+            wl["L"] = (args.size[0], args.size[1], args.size[2] + 2)
+        workload_name = (f"{args.algorithm.upper()} Poiseuille channel {wl['L'][0]}x{wl['L'][1]}x{wl['L'][2] - 2} "
+                         f"cells (+2 wall layers in z), n={wl['n']}, T=1, g=0.001, dt=0.02, Philox seed 0")
     h = capi.Handle(L=wl["L"], periodic=wl["periodic"], n=wl["n"], dt=wl["dt"], drag=wl["drag"],
-                    temperature=wl["temperature"], seed=wl["seed"] + rank, device_id=local_rank)
+                    temperature=wl["temperature"], algorithm=algorithm, seed=wl["seed"] + rank,
+                    device_id=local_rank)
     N, C = h.N, h.C
     h.step(args.warmup)
     h.synchronize()
@@ -206,34 +256,9 @@ def run_gpu_arm(args, rank, world, local_rank):
     value = world * N * args.steps / (elapsed * 1e-3)
 
     # end to end through the Python API: step_and_sample + get_mean_fields
-    import cudampcd_gb300 as pympcd
-
-    params = pympcd.Params()
-    params.n = wl["n"]
-    params.temperature = wl["temperature"]
-    params.volume_size = (wl["L"][0], wl["L"][1], wl["L"][2] - 2)
-    params.periodicity = wl["periodic"]
-    params.drag = wl["drag"]
-    params.delta_t = wl["dt"]
-    params.algorithm = "srd"
-    params.device_id = local_rank
-    params.seed = wl["seed"] + rank
-    sim = pympcd.Simulation(params, "cuda")
-    sim.step_and_sample(min(args.warmup, 5))
-    sim.get_mean_fields()
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    sim.step_and_sample(args.steps)
-    density, velocity = sim.get_mean_fields()
-    e2e_s = time.perf_counter() - t0
-    del sim
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * N * args.steps / e2e_s
-    d2h = (density.nbytes + velocity.nbytes) / args.steps
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, wl, algorithm, rank, local_rank, dist, world, N)
 
     if rank == 0:
         peak, peak_kind = peaks()
@@ -245,17 +270,16 @@ def run_gpu_arm(args, rank, world, local_rank):
             "warmup": args.warmup, "ms_per_step": elapsed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": value / (world * REFERENCE_PUBLISHED), "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD_NAME, "particles_per_gpu": N, "cells_per_gpu": C,
+            "config": {"workload": workload_name, "particles_per_gpu": N, "cells_per_gpu": C,
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "l2": "inputs larger than L2: 25.6 GB of particle state read and written per step",
+                       "l2": f"inputs larger than L2: {64 * N / 1e9:.1f} GB of particle state read and written per step",
                        "vs_baseline_ref": "reference README.md:41, 94 ms/step on an Ampere GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": bpp * N if bpp else None, "traffic_source": src,
                          "algorithmic_bytes_per_particle": ALGO_BYTES_PER_PARTICLE,
-                         "kernel": "step_kernel<SRD, Philox>", "kernel_ms": per_launch_ms},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,
-                    "api": "cudampcd_gb300.Simulation.step_and_sample + get_mean_fields (host wall clock)"},
+                         "kernel": f"step_kernel<{args.algorithm.upper()}, Philox>", "kernel_ms": per_launch_ms},
+            "e2e": e2e,
             "clocks": clocks.summary(),
             "gpu_launches": args.steps,
             "device_counters": {"bucket_overflows": overflowed, "error_flags": flags},
@@ -280,6 +304,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--steps-cpu", dest="steps_cpu", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--size", type=int, nargs=3, metavar=("LX", "LY", "LZ"))
+    ap.add_argument("--algorithm", default="srd", choices=["srd", "extended"])
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")

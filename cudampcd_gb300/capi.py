@@ -71,6 +71,16 @@ def lib() -> C.CDLL:
         L.mpcd_gb_inject_draws.argtypes = [H, C.c_uint32, C.c_uint32] + [C.c_void_p] * 6
         L.mpcd_gb_counters.argtypes = [H, u64p]
         L.mpcd_gb_cell_offsets_noalloc.argtypes = [H, C.c_void_p, C.c_uint64]
+        L.mpcd_gb_ensemble_create.argtypes = [C.c_void_p, C.c_int32, C.POINTER(H)]
+        L.mpcd_gb_num_boxes.argtypes = [H]
+        L.mpcd_gb_box_range.argtypes = [H, C.c_int32, u64p]
+        L.mpcd_gb_set_particles_device.argtypes = [H, C.c_void_p, C.c_void_p]
+        L.mpcd_gb_get_particles_device.argtypes = [H, C.c_void_p, C.c_void_p]
+        L.mpcd_gb_set_drag.argtypes = [H, C.c_float]
+        L.mpcd_gb_profile_forward.argtypes = [H, C.c_int32, C.c_int32, C.c_void_p]
+        L.mpcd_gb_profile_backward.argtypes = [H, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+        L.mpcd_gb_profile_tape.argtypes = [H] + [C.c_void_p] * 5
+        L.mpcd_gb_autotune.argtypes = [H, C.c_int32, np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")]
         _lib = L
     return _lib
 
@@ -79,26 +89,53 @@ class GbError(RuntimeError):
     pass
 
 
+def make_params(L=(10, 10, 10), periodic=(1, 1, 1), n=10, dt=0.02, drag=0.0, temperature=1.0, algorithm=0,
+                experiment=0, seed=0, device_id=0) -> Params:
+    p = Params()
+    p.experiment, p.algorithm, p.collision_kernel = experiment, algorithm, 2
+    p.periodicity[:] = [int(v) for v in periodic]
+    p.volume_size[:] = [float(v) for v in L]
+    p.n, p.device_id = n, device_id
+    p.delta_t, p.temperature, p.thermal_velocity, p.drag = dt, temperature, float(np.sqrt(temperature)), drag
+    p.seed = seed
+    return p
+
+
 class Handle:
     """One simulation behind the C ABI."""
 
     def __init__(self, L=(10, 10, 10), periodic=(1, 1, 1), n=10, dt=0.02, drag=0.0, temperature=1.0,
-                 algorithm=0, experiment=0, seed=0, device_id=0):
+                 algorithm=0, experiment=0, seed=0, device_id=0, boxes=None):
+        """One box from the keyword arguments, or a batched ensemble from
+        `boxes`, a list of dicts with the same keywords (one per box)."""
         self._lib = lib()
-        p = Params()
-        p.experiment, p.algorithm, p.collision_kernel = experiment, algorithm, 2
-        p.periodicity[:] = [int(v) for v in periodic]
-        p.volume_size[:] = [float(v) for v in L]
-        p.n, p.device_id = n, device_id
-        p.delta_t, p.temperature, p.thermal_velocity, p.drag = dt, temperature, float(np.sqrt(temperature)), drag
-        p.seed = seed
-        self.params = p
+        if boxes is None:
+            boxes = [dict(L=L, periodic=periodic, n=n, dt=dt, drag=drag, temperature=temperature,
+                          algorithm=algorithm, experiment=experiment, seed=seed, device_id=device_id)]
+        plist = [make_params(**b) for b in boxes]
+        arr = (Params * max(1, len(plist)))(*plist)
+        self.params = plist[0] if plist else None
         self.h = C.c_void_p()
-        rc = self._lib.mpcd_gb_create(C.byref(p), C.byref(self.h))
+        rc = self._lib.mpcd_gb_ensemble_create(C.cast(arr, C.c_void_p), len(plist), C.byref(self.h))
         if rc != 0:
             raise GbError(f"mpcd_gb_create failed ({rc}): {self._lib.mpcd_gb_last_error(None).decode()}")
         self.N = int(self._lib.mpcd_gb_num_particles(self.h))
         self.C = int(self._lib.mpcd_gb_num_cells(self.h))
+
+    @property
+    def num_boxes(self):
+        return int(self._lib.mpcd_gb_num_boxes(self.h))
+
+    def box_range(self, r):
+        """(first_particle, num_particles, first_cell, num_cells) of box r."""
+        out = np.zeros(4, np.uint64)
+        self._check(self._lib.mpcd_gb_box_range(self.h, r, out))
+        return tuple(int(v) for v in out)
+
+    def autotune(self, steps_per_candidate=3):
+        out = np.zeros(2, np.uint32)
+        self._check(self._lib.mpcd_gb_autotune(self.h, steps_per_candidate, out))
+        return int(out[0]), int(out[1])
 
     def _check(self, rc):
         if rc != 0:
@@ -189,6 +226,38 @@ class Handle:
         """Queue the cell offsets of the current layout into the device buffer at
         address d_offsets (n_offsets uint32 entries) on the handle's stream."""
         self._check(self._lib.mpcd_gb_cell_offsets_noalloc(self.h, C.c_void_p(d_offsets), n_offsets))
+
+    # device-pointer I/O and the differentiable profile (addresses of device buffers)
+    def set_particles_device(self, d_pos, d_vel):
+        self._check(self._lib.mpcd_gb_set_particles_device(self.h, C.c_void_p(d_pos or None),
+                                                           C.c_void_p(d_vel or None)))
+
+    def get_particles_device(self, d_pos, d_vel):
+        self._check(self._lib.mpcd_gb_get_particles_device(self.h, C.c_void_p(d_pos or None),
+                                                           C.c_void_p(d_vel or None)))
+
+    def set_drag(self, drag):
+        self._check(self._lib.mpcd_gb_set_drag(self.h, float(drag)))
+
+    def profile_forward(self, steps, every, d_profile):
+        self._check(self._lib.mpcd_gb_profile_forward(self.h, steps, every, C.c_void_p(d_profile)))
+
+    def profile_backward(self, d_grad_profile, d_grad_vel):
+        g = C.c_double()
+        self._check(self._lib.mpcd_gb_profile_backward(self.h, C.c_void_p(d_grad_profile), C.c_void_p(d_grad_vel),
+                                                       C.byref(g)))
+        return g.value
+
+    def profile_tape(self, steps):
+        """Fixed events of the last profile forward: (key, lab, ncell, lab_count, bounce0)."""
+        key = np.zeros((steps, self.N), np.uint32)
+        lab = np.zeros((steps, self.N), np.uint32)
+        ncell = np.zeros((steps, self.C), np.uint32)
+        cnt = np.zeros((steps, self.C), np.uint32)
+        b0 = np.zeros(self.N, np.uint32)
+        self._check(self._lib.mpcd_gb_profile_tape(self.h, key.ctypes.data, lab.ctypes.data, ncell.ctypes.data,
+                                                   cnt.ctypes.data, b0.ctypes.data))
+        return key, lab, ncell, cnt, b0
 
     def set_stream(self, stream_ptr):
         self._check(self._lib.mpcd_gb_set_stream(self.h, C.c_void_p(stream_ptr)))

@@ -1,6 +1,7 @@
 // Host engine of the GB300 MPCD step and the C ABI of include/mpcd_gb.h.
 //
-// One handle = one simulation on one GPU: its device buffers, one CUDA stream,
+// One handle = one simulation on one GPU (or a batched ensemble of independent
+// boxes advanced by the same launches): its device buffers, one CUDA stream,
 // the step counter that keys every Philox draw, and the sampling state machine
 // of the reference (cuda_backend_impl.cu:182-218).  No call synchronises
 // except the getters, the sample read-out and the error check at the end of
@@ -98,14 +99,16 @@ void check(cudaError_t e, const char* what)
 
 class Engine {
 public:
-    explicit Engine(const mpcd_gb_params& p) : params_(p)
+    // R boxes (R = 1: a plain simulation); every box has its own geometry,
+    // density, drag, temperature, time step and seed, all share the algorithm.
+    Engine(const mpcd_gb_params* ps, int R) : params_(ps[0]), box_params_(ps, ps + R)
     {
         validate();
-        check(cudaSetDevice((int)p.device_id), "cudaSetDevice");
+        check(cudaSetDevice((int)params_.device_id), "cudaSetDevice");
         check(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking), "cudaStreamCreate");
         stream_ = own_stream_;
         cudaDeviceProp prop;
-        check(cudaGetDeviceProperties(&prop, (int)p.device_id), "cudaGetDeviceProperties");
+        check(cudaGetDeviceProperties(&prop, (int)params_.device_id), "cudaGetDeviceProperties");
         sms_ = prop.multiProcessorCount;
         build_boxes();
         allocate();
@@ -115,6 +118,7 @@ public:
 
     ~Engine()
     {
+        for (auto& g : graph_) g.reset();
         if (own_stream_) {
             cudaStreamSynchronize(own_stream_);
             cudaStreamDestroy(own_stream_);
@@ -125,8 +129,15 @@ public:
     void step(int n, bool sample)
     {
         if (n < 0) throw Error(MPCD_GB_EINVAL, "negative step count");
-        for (int i = 0; i < n; ++i) {
+        for (int i = 0; i < n;) {
             const bool snapshot = sample && !sampling_;
+            if (graphs_ && !snapshot && !use_table_ && step_ % kGraphSteps == 0 && n - i >= kGraphSteps) {
+                const int done = replay_graph(sample, (n - i) / kGraphSteps);
+                i += done;
+                if (sample) sample_counter_ += (uint64_t)done;
+                continue;
+            }
+            ++i;
             launch_one_step(sample);
             if (sample) {
                 check(launch_sample_finalize(samp_.as<float4>(), acc_.as<SampleAcc>(), cells_, snapshot ? 1 : 0,
@@ -151,8 +162,7 @@ public:
         check(cudaStreamSynchronize(stream_), "sample read");
         // cpu_backend.cpp:218 / cuda_backend_impl.cu:210: divide by the counter, S-1 for S samples
         const double inverse = 1.0 / (double)sample_counter_;
-        const BoxDesc& b = boxes_[0];
-        for (uint32_t c = 0; c < b.C; ++c) {
+        for (uint64_t c = 0; c < cells_; ++c) {   // lab cells of every box, each in reference order
             density[c] = (float)(acc[c].n * inverse);
             velocity[3 * c + 0] = (float)(acc[c].vx * inverse);
             velocity[3 * c + 1] = (float)(acc[c].vy * inverse);
@@ -209,14 +219,151 @@ public:
                                   stream_),
                   "dump");
             check(cudaStreamSynchronize(stream_), "dump");
-            const BoxDesc& b = boxes_[0];
-            for (uint32_t s = 0; s < b.C; ++s) {
-                const uint32_t Lz = (uint32_t)b.L[2], Lx = (uint32_t)b.L[0];
-                const uint32_t z = s % Lz, col = s / Lz, x = col % Lx, y = col / Lx;
-                counts[x + Lx * (y + (uint32_t)b.L[1] * z)] = raw[s];
-            }
+            for (const BoxDesc& b : boxes_)
+                for (uint32_t s = 0; s < b.C; ++s) {
+                    const uint32_t Lz = (uint32_t)b.L[2], Lx = (uint32_t)b.L[0];
+                    const uint32_t z = s % Lz, col = s / Lz, x = col % Lx, y = col / Lx;
+                    counts[b.cell_base + x + Lx * (y + (uint32_t)b.L[1] * z)] = raw[b.cell_base + s];
+                }
         }
         check(cudaStreamSynchronize(stream_), "dump");
+    }
+
+    // ------------------------------------------------------------ device-pointer I/O, drag
+    void set_device(const float* d_pos, const float* d_vel)
+    {
+        if (!d_pos || !d_vel) materialise();
+        if (d_pos)
+            check(cudaMemcpyAsync(dense_pos_.p, d_pos, sizeof(float) * 3 * N_, cudaMemcpyDeviceToDevice, stream_),
+                  "positions write");
+        if (d_vel)
+            check(cudaMemcpyAsync(dense_vel_.p, d_vel, sizeof(float) * 3 * N_, cudaMemcpyDeviceToDevice, stream_),
+                  "velocities write");
+        scatter_dense();
+        check_device_errors();
+    }
+
+    void get_device(float* d_pos, float* d_vel)
+    {
+        materialise();
+        if (d_pos)
+            check(cudaMemcpyAsync(d_pos, dense_pos_.p, sizeof(float) * 3 * N_, cudaMemcpyDeviceToDevice, stream_),
+                  "positions read");
+        if (d_vel)
+            check(cudaMemcpyAsync(d_vel, dense_vel_.p, sizeof(float) * 3 * N_, cudaMemcpyDeviceToDevice, stream_),
+                  "velocities read");
+        check(cudaStreamSynchronize(stream_), "particle read");
+    }
+
+    // Body force of every box from the next step on.
+    void set_drag(float drag)
+    {
+        if (!std::isfinite(drag)) throw Error(MPCD_GB_EINVAL, "drag must be finite");
+        if (step_ > 0) materialise();   // a later replay of the last step must still use its drag
+        for (size_t r = 0; r < boxes_.size(); ++r) {
+            box_params_[r].drag = drag;
+            boxes_[r].drag_dt = drag * boxes_[r].dt;
+        }
+        params_.drag = drag;
+        check(cudaStreamSynchronize(stream_), "set drag");
+        check(cudaMemcpy(boxes_d_.p, boxes_.data(), sizeof(BoxDesc) * boxes_.size(), cudaMemcpyHostToDevice),
+              "upload boxes");
+        for (auto& g : graph_) g.reset();
+    }
+
+    // ------------------------------------------------------------ adjoint of the sampled profile
+    //
+    // Forward: from the current state, `steps` sampled steps; the dense state is
+    // checkpointed every `every` steps.  Backward: per segment, last first,
+    // restore its checkpoint, recompute its steps recording the tape (the draws
+    // are replayed from the Philox counters, the recomputation is bit-identical),
+    // then run the reverse sweep over them.
+    void profile_forward(int steps, int every, float* d_profile)
+    {
+        if (boxes_.size() != 1 || params_.algorithm != 0)
+            throw Error(MPCD_GB_ESTATE, "the profile adjoint needs a single-box SRD handle");
+        if (steps < 1 || every < 1) throw Error(MPCD_GB_EINVAL, "steps and checkpoint interval must be positive");
+        if (!d_profile) throw Error(MPCD_GB_EINVAL, "null profile buffer");
+        if (use_table_) throw Error(MPCD_GB_ESTATE, "injected draws pending");
+        const int nseg = (steps + every - 1) / every;
+        const size_t per = sizeof(float) * 6 * N_;
+        if (ckpt_.bytes < per * nseg) check(ckpt_.alloc(per * nseg), "alloc checkpoints");
+        adj_valid_ = false;
+        adj_s0_ = step_;
+        adj_steps_ = steps;
+        adj_every_ = every;
+        sampling_ = false;
+        for (int j = 0; j < nseg; ++j) {
+            materialise();
+            char* c = static_cast<char*>(ckpt_.p) + per * j;
+            check(cudaMemcpyAsync(c, dense_pos_.p, per / 2, cudaMemcpyDeviceToDevice, stream_), "checkpoint");
+            check(cudaMemcpyAsync(c + per / 2, dense_vel_.p, per / 2, cudaMemcpyDeviceToDevice, stream_),
+                  "checkpoint");
+            step(std::min(every, steps - j * every), true);
+        }
+        check(launch_profile(acc_.as<SampleAcc>(), boxes_[0], (uint64_t)steps, d_profile, stream_), "profile");
+        check(cudaStreamSynchronize(stream_), "profile");
+        adj_valid_ = true;
+    }
+
+    void profile_backward(const float* d_dU, float* d_dv0, double* ddrag)
+    {
+        if (!adj_valid_) throw Error(MPCD_GB_ESTATE, "no profile forward to differentiate");
+        if (!d_dU || !d_dv0 || !ddrag) throw Error(MPCD_GB_EINVAL, "null argument");
+        const BoxDesc& b = boxes_[0];
+        alloc_tape();
+        check(cudaMemsetAsync(lam_.p, 0, lam_.bytes, stream_), "adjoint");
+        check(cudaMemsetAsync(gsum_.p, 0, gsum_.bytes, stream_), "adjoint");
+        const int nseg = (adj_steps_ + adj_every_ - 1) / adj_every_;
+        for (int j = nseg - 1; j >= 0; --j) {
+            const int k = record_segment(j);
+            for (int i = k - 1; i >= 0; --i) {
+                const uint64_t t = adj_s0_ + (uint64_t)j * adj_every_ + i;
+                check(launch_adjoint_step(b, t, (uint64_t)adj_steps_, lam_.as<float>(),
+                                          tkey_.as<uint32_t>() + (size_t)i * N_, tlab_.as<uint32_t>() + (size_t)i * N_,
+                                          tncell_.as<uint32_t>() + (size_t)i * cells_,
+                                          tcnt_.as<uint32_t>() + (size_t)i * cells_, d_dU, cellsum_.as<float4>(),
+                                          gsum_.as<double>(), sms_ * 8, stream_),
+                      "adjoint step");
+            }
+        }
+        check(launch_adjoint_finish((uint32_t)N_, lam_.as<float>(), tb0_.as<uint32_t>(), d_dv0, sms_ * 8, stream_),
+              "adjoint");
+        double g = 0;
+        check(cudaMemcpyAsync(&g, gsum_.p, sizeof g, cudaMemcpyDeviceToHost, stream_), "adjoint");
+        check(cudaStreamSynchronize(stream_), "adjoint");
+        check_device_errors();
+        *ddrag = g * (double)b.dt;
+        sampling_ = false;
+    }
+
+    // Test hook: the tape of every step of the last profile forward (host arrays
+    // of steps * N, steps * N, steps * C, steps * C and N entries).
+    void profile_tape(uint32_t* key, uint32_t* lab, uint32_t* ncell, uint32_t* lab_count, uint32_t* bounce0)
+    {
+        if (!adj_valid_) throw Error(MPCD_GB_ESTATE, "no profile forward recorded");
+        alloc_tape();
+        const int nseg = (adj_steps_ + adj_every_ - 1) / adj_every_;
+        for (int j = 0; j < nseg; ++j) {
+            const int k = record_segment(j);
+            const size_t t0 = (size_t)j * adj_every_;
+            auto down = [&](uint32_t* dst, const DeviceBuffer& src, size_t per) {
+                if (dst)
+                    check(cudaMemcpyAsync(dst + t0 * per, src.p, sizeof(uint32_t) * per * k, cudaMemcpyDeviceToHost,
+                                          stream_),
+                          "tape read");
+            };
+            down(key, tkey_, N_);
+            down(lab, tlab_, N_);
+            down(ncell, tncell_, cells_);
+            down(lab_count, tcnt_, cells_);
+            if (j == 0 && bounce0)
+                check(cudaMemcpyAsync(bounce0, tb0_.p, sizeof(uint32_t) * N_, cudaMemcpyDeviceToHost, stream_),
+                      "tape read");
+            check(cudaStreamSynchronize(stream_), "tape read");
+        }
+        check_device_errors();
+        sampling_ = false;
     }
 
     // Cell offsets of the current layout into a caller's device buffer; the
@@ -299,6 +446,7 @@ public:
             use_table_ = false;
             return;
         }
+        if (boxes_.size() != 1) throw Error(MPCD_GB_ESTATE, "injected draws need a single-box handle");
         const size_t C = boxes_[0].C;
         check(t_count_.alloc(sizeof(uint32_t) * C), "draws alloc");
         check(t_gpos_.alloc(sizeof(float) * C * gmax * 3 + 16), "draws alloc");
@@ -365,15 +513,74 @@ public:
     }
 
     size_t num_particles() const { return N_; }
-    size_t num_cells() const { return boxes_[0].C; }
+    size_t num_cells() const { return cells_; }
     uint64_t step_index() const { return step_; }
+    int num_boxes() const { return (int)boxes_.size(); }
+
+    void box_range(int r, uint64_t out[4]) const
+    {
+        if (r < 0 || r >= (int)boxes_.size()) throw Error(MPCD_GB_EINVAL, "box index out of range");
+        const BoxDesc& b = boxes_[(size_t)r];
+        out[0] = b.dense_base;
+        out[1] = b.N;
+        out[2] = b.cell_base;
+        out[3] = b.C;
+    }
+
+    // Time `steps` real steps of every admissible (tile cells, buffer) pair and
+    // keep the fastest; the steps advance the simulation like any others.
+    void autotune(int steps, uint32_t out[2])
+    {
+        if (steps < 1) throw Error(MPCD_GB_EINVAL, "autotune needs at least one step per candidate");
+        uint32_t n_max = 0;
+        for (const BoxDesc& b : boxes_) n_max = std::max(n_max, b.n);
+        cudaEvent_t e0, e1;
+        check(cudaEventCreate(&e0), "event");
+        check(cudaEventCreate(&e1), "event");
+        float best = -1.0f;
+        uint32_t best_tc = boxes_[0].tile_cells, best_pbuf = pbuf_;
+        for (uint32_t pbuf : {1024u, 1536u, 2048u}) {
+            if (pbuf < 5 * n_max) continue;
+            for (uint32_t tc = 8; tc <= 128; tc <<= 1) {
+                if (tc * n_max > pbuf) continue;
+                retile(tc, pbuf);
+                launch_one_step(false);   // first launch of a configuration: not timed
+                check(cudaEventRecord(e0, stream_), "event");
+                for (int i = 0; i < steps; ++i) launch_one_step(false);
+                check(cudaEventRecord(e1, stream_), "event");
+                check(cudaEventSynchronize(e1), "event");
+                float ms = 0;
+                check(cudaEventElapsedTime(&ms, e0, e1), "event");
+                check_device_errors();
+                if (best < 0 || ms < best) {
+                    best = ms;
+                    best_tc = tc;
+                    best_pbuf = pbuf;
+                }
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        retile(best_tc, best_pbuf);
+        out[0] = best_tc;
+        out[1] = best_pbuf;
+    }
 
 private:
     unsigned parity() const { return (unsigned)(step_ & 1); }
 
     void validate()
     {
-        const mpcd_gb_params& p = params_;
+        if (box_params_.empty()) throw Error(MPCD_GB_EINVAL, "an ensemble needs at least one box");
+        for (const mpcd_gb_params& p : box_params_) {
+            validate_one(p);
+            if (p.algorithm != params_.algorithm) throw Error(MPCD_GB_EINVAL, "all boxes must use the same algorithm");
+            if (p.device_id != params_.device_id) throw Error(MPCD_GB_EINVAL, "all boxes must use the same device");
+        }
+    }
+
+    static void validate_one(const mpcd_gb_params& p)
+    {
         for (int d = 0; d < 3; ++d) {
             const float L = p.volume_size[d];
             if (!(L >= 1.0f) || L != std::floor(L) || L > 65536.0f)
@@ -391,9 +598,8 @@ private:
         if (!std::isfinite(p.drag)) throw Error(MPCD_GB_EINVAL, "drag must be finite");
     }
 
-    void build_boxes()
+    static BoxDesc make_box(const mpcd_gb_params& p)
     {
-        const mpcd_gb_params& p = params_;
         BoxDesc b{};
         uint64_t Nf = p.n;
         for (int d = 0; d < 3; ++d) {
@@ -418,41 +624,54 @@ private:
         if (Nf >= (1ull << 32) - 1) throw Error(MPCD_GB_EINVAL, "too many particles");
         b.C = (uint32_t)C;
         b.N = (uint32_t)Nf;
-        b.cell_base = 0;
-        b.slot_base = 0;
-        b.dense_base = 0;
         b.div_z = ((1ull << 48) + (uint64_t)b.L[2] - 1) / (uint64_t)b.L[2];
         b.div_x = ((1ull << 48) + (uint64_t)b.L[0] - 1) / (uint64_t)b.L[0];
         b.seed_lo = (uint32_t)p.seed;
         b.seed_hi = (uint32_t)(p.seed >> 32);
+        return b;
+    }
+
+    void build_boxes()
+    {
+        boxes_.clear();
+        uint64_t cells = 0, slots = 0, particles = 0;
+        uint32_t n_max = 0;
+        for (const mpcd_gb_params& p : box_params_) {
+            BoxDesc b = make_box(p);
+            if (cells + b.C >= (1ull << 31)) throw Error(MPCD_GB_EINVAL, "too many cells in the ensemble");
+            b.cell_base = (uint32_t)cells;
+            b.slot_base = slots;
+            b.dense_base = particles;
+            cells += b.C;
+            slots += (uint64_t)b.C * b.cap;
+            particles += b.N;
+            n_max = std::max(n_max, b.n);
+            boxes_.push_back(b);
+        }
+        if (particles >= (1ull << 32) - 1) throw Error(MPCD_GB_EINVAL, "too many particles in the ensemble");
+        N_ = particles;
+        cells_ = cells;
+        total_slots_ = slots;
+        ov_cap_ = (uint32_t)std::max<uint64_t>(1u << 16, std::min<uint64_t>(N_, 1u << 22));
+        if (total_slots_ + ov_cap_ >= (1ull << 32))
+            throw Error(MPCD_GB_EINVAL, "cells * 4n exceeds the 32-bit slot space of one handle");
         // tile: a power-of-two number of cells (a group of 256 / cells threads per
         // cell), about 1300 particles; the buffer holds one cell with all its
         // ghosts (cap + n = 5n) at least
-        pbuf_ = 1536;
-        if (5 * b.n > pbuf_) pbuf_ = 5 * b.n;
-        if (pbuf_ > 2048) throw Error(MPCD_GB_EINVAL, "n above 409: one cell and its ghosts must fit a tile");
+        uint32_t pbuf = std::max(1536u, 5 * n_max);
+        if (pbuf > 2048) throw Error(MPCD_GB_EINVAL, "n above 409: one cell and its ghosts must fit a tile");
         uint32_t tc = 128;
-        while (tc > 8 && tc * b.n * 1.15 > pbuf_) tc >>= 1;
-        // tuning overrides (used by the autotuner and the tuning sweeps)
+        while (tc > 8 && tc * n_max * 1.15 > pbuf) tc >>= 1;
+        // tuning overrides (used by the tuning sweeps)
         if (const char* e = std::getenv("MPCD_GB_PBUF")) {
             const uint32_t v = (uint32_t)std::strtoul(e, nullptr, 10);
-            if (v >= 5 * b.n && v <= 2048) pbuf_ = v;
+            if (v >= 5 * n_max && v <= 2048) pbuf = v;
         }
         if (const char* e = std::getenv("MPCD_GB_TILE_CELLS")) {
             const uint32_t v = (uint32_t)std::strtoul(e, nullptr, 10);
             if (v >= 1 && v <= 256 && (v & (v - 1)) == 0) tc = v;
         }
-        b.tile_cells = tc;
-        b.tile_base = 0;
-        b.tiles = (b.C + tc - 1) / tc;
-        boxes_.assign(1, b);
-        N_ = Nf;
-        cells_ = C;
-        tiles_ = b.tiles;
-        total_slots_ = C * b.cap;
-        ov_cap_ = (uint32_t)std::max<uint64_t>(1u << 16, std::min<uint64_t>(N_, 1u << 22));
-        if (total_slots_ + ov_cap_ >= (1ull << 32))
-            throw Error(MPCD_GB_EINVAL, "cells * 4n exceeds the 32-bit slot space of one handle");
+        set_tiles(tc, pbuf);
         float table[13][3];
         const int steps = 4;
         for (int select = 0; select <= 12; ++select) {   // simulation_functions.cpp:272-290
@@ -468,6 +687,30 @@ private:
             table[select][2] = cosf(theta);
         }
         std::memcpy(ext_axis_, table, sizeof table);
+    }
+
+    // Work decomposition only: buckets are per cell, so tiles can change between steps.
+    void set_tiles(uint32_t tc, uint32_t pbuf)
+    {
+        uint64_t tiles = 0;
+        for (BoxDesc& b : boxes_) {
+            b.tile_cells = tc;
+            b.tile_base = (uint32_t)tiles;
+            b.tiles = (b.C + tc - 1) / tc;
+            tiles += b.tiles;
+        }
+        tiles_ = tiles;
+        pbuf_ = pbuf;
+        for (auto& g : graph_) g.reset();   // graphs bake the tiling into their launches
+    }
+
+    void retile(uint32_t tc, uint32_t pbuf)
+    {
+        check(cudaStreamSynchronize(stream_), "retile");
+        set_tiles(tc, pbuf);
+        check(cudaMemcpy(boxes_d_.p, boxes_.data(), sizeof(BoxDesc) * boxes_.size(), cudaMemcpyHostToDevice),
+              "upload boxes");
+        configure();
     }
 
     void allocate()
@@ -496,7 +739,7 @@ private:
         check(offsets_.alloc(sizeof(uint32_t) * (cells_ + 1)), "alloc offsets");
         check(scan_status_.alloc(sizeof(unsigned long long) * scan_status_words(cells_)), "alloc scan status");
         check(scan_counter_.alloc(sizeof(unsigned int)), "alloc scan counter");
-        check(partial_.alloc(sizeof(double) * 3 * kReduceBlocks), "alloc partial sums");
+        check(partial_.alloc(sizeof(double) * 3 * kReduceBlocks * boxes_.size()), "alloc partial sums");
     }
 
     void configure()
@@ -512,20 +755,27 @@ private:
         check(launch_init(boxes_d_.as<BoxDesc>(), (int)boxes_.size(), dense_pos_.as<float>(), dense_vel_.as<float>(),
                           N_, sms_ * 16, stream_),
               "init");
-        // zero net momentum (BASELINE config 1 asks for it; the reference does not remove it)
-        check(launch_momentum_partial(dense_vel_.as<float>(), 0, N_, partial_.as<double>(), kReduceBlocks, stream_),
-              "momentum");
-        std::vector<double> part(3 * kReduceBlocks);
+        // zero net momentum in every box (the reference does not remove it)
+        for (size_t r = 0; r < boxes_.size(); ++r) {
+            const BoxDesc& b = boxes_[r];
+            check(launch_momentum_partial(dense_vel_.as<float>(), b.dense_base, b.dense_base + b.N,
+                                          partial_.as<double>() + 3 * kReduceBlocks * r, kReduceBlocks, stream_),
+                  "momentum");
+        }
+        std::vector<double> part(3 * kReduceBlocks * boxes_.size());
         check(cudaMemcpyAsync(part.data(), partial_.p, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, stream_),
               "momentum");
         check(cudaStreamSynchronize(stream_), "momentum");
-        double m[3] = {0, 0, 0};
-        for (int i = 0; i < kReduceBlocks; ++i)
-            for (int d = 0; d < 3; ++d) m[d] += part[3 * i + d];
-        if (N_)
-            check(launch_subtract(dense_vel_.as<float>(), 0, N_, (float)(m[0] / N_), (float)(m[1] / N_),
-                                  (float)(m[2] / N_), sms_ * 16, stream_),
-                  "momentum");
+        for (size_t r = 0; r < boxes_.size(); ++r) {
+            const BoxDesc& b = boxes_[r];
+            double m[3] = {0, 0, 0};
+            for (int i = 0; i < kReduceBlocks; ++i)
+                for (int d = 0; d < 3; ++d) m[d] += part[3 * kReduceBlocks * r + 3 * i + d];
+            if (b.N)
+                check(launch_subtract(dense_vel_.as<float>(), b.dense_base, b.dense_base + b.N, (float)(m[0] / b.N),
+                                      (float)(m[1] / b.N), (float)(m[2] / b.N), sms_ * 16, stream_),
+                      "momentum");
+        }
         scatter_dense();
         check(cudaStreamSynchronize(stream_), "initialise");
         check_device_errors();
@@ -570,6 +820,74 @@ private:
         return a;
     }
 
+    // ------------------------------------------------------------ step graphs
+    //
+    // kGraphSteps consecutive steps (buffer parity repeats every 2 steps, the
+    // count rotation every 3) captured once per variant (with or without
+    // sampling) and replayed from any step that is a multiple of kGraphSteps:
+    // every kernel of the graph reads its absolute step from state->step_base,
+    // and the graph's last node advances it.
+    static constexpr int kGraphSteps = 6;
+
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        ~StepGraph() { reset(); }
+        void reset()
+        {
+            if (exec) cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
+    };
+
+    unsigned long long* step_base_ptr() const
+    {
+        return reinterpret_cast<unsigned long long*>(static_cast<char*>(state_.p) + offsetof(DeviceState, step_base));
+    }
+
+    cudaGraphExec_t step_graph(bool sample)
+    {
+        StepGraph& g = graph_[sample ? 1 : 0];
+        if (g.exec) return g.exec;
+        cudaStream_t cs = own_stream_;
+        check(cudaStreamSynchronize(cs), "graph capture");
+        check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "graph capture");
+        cudaError_t err = cudaSuccess;
+        for (int i = 0; i < kGraphSteps && err == cudaSuccess; ++i) {
+            StepArgs a = args((uint64_t)i);   // buffers of step i == those of any step = i mod 6
+            a.step_base = step_base_ptr();
+            a.sample = sample ? 1 : 0;
+            err = launch_step(a, params_.algorithm, false, pbuf_, grid_, cs);
+            if (err == cudaSuccess && sample)
+                err = launch_sample_finalize(samp_.as<float4>(), acc_.as<SampleAcc>(), cells_, 0, sms_ * 8, cs);
+        }
+        if (err == cudaSuccess) err = launch_advance(state_.as<DeviceState>(), kGraphSteps, cs);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t end = cudaStreamEndCapture(cs, &graph);
+        if (err == cudaSuccess) err = end;
+        if (err == cudaSuccess) err = cudaGraphInstantiate(&g.exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (err != cudaSuccess) g.reset();
+        check(err, "step graph");
+        return g.exec;
+    }
+
+    // reps replays of the step graph from step step_ (a multiple of kGraphSteps);
+    // returns the steps run.
+    int replay_graph(bool sample, int reps)
+    {
+        cudaGraphExec_t g = step_graph(sample);
+        graph_base_host_ = step_;
+        check(cudaMemcpyAsync(step_base_ptr(), &graph_base_host_, sizeof graph_base_host_, cudaMemcpyHostToDevice,
+                              stream_),
+              "graph step base");
+        for (int r = 0; r < reps; ++r) check(cudaGraphLaunch(g, stream_), "graph launch");
+        const int done = reps * kGraphSteps;
+        step_ += (uint64_t)done;
+        last_step_table_ = false;
+        dense_valid_ = false;
+        return done;
+    }
+
     void launch_one_step(bool sample)
     {
         StepArgs a = args(step_);
@@ -596,9 +914,53 @@ private:
         }
     }
 
+    void alloc_tape()
+    {
+        const size_t K = (size_t)adj_every_;
+        auto need = [&](DeviceBuffer& d, size_t bytes, const char* what) {
+            if (d.bytes < bytes) check(d.alloc(bytes), what);
+        };
+        need(tkey_, sizeof(uint32_t) * N_ * K, "alloc tape");
+        need(tlab_, sizeof(uint32_t) * N_ * K, "alloc tape");
+        need(tncell_, sizeof(uint32_t) * cells_ * K, "alloc tape");
+        need(tcnt_, sizeof(uint32_t) * cells_ * K, "alloc tape");
+        need(tb0_, sizeof(uint32_t) * N_, "alloc tape");
+        need(lam_, sizeof(float) * 3 * N_, "alloc adjoint");
+        need(cellsum_, sizeof(float4) * cells_, "alloc adjoint");
+        need(gsum_, sizeof(double), "alloc adjoint");
+    }
+
+    // Restore checkpoint j and recompute its steps with the tape recorded
+    // (slot i of the tape = step s0 + j * every + i); returns the steps run.
+    int record_segment(int j)
+    {
+        const int k = std::min(adj_every_, adj_steps_ - j * adj_every_);
+        const size_t per = sizeof(float) * 6 * N_;
+        const char* c = static_cast<const char*>(ckpt_.p) + per * j;
+        check(cudaMemcpyAsync(dense_pos_.p, c, per / 2, cudaMemcpyDeviceToDevice, stream_), "restore");
+        check(cudaMemcpyAsync(dense_vel_.p, c + per / 2, per / 2, cudaMemcpyDeviceToDevice, stream_), "restore");
+        step_ = adj_s0_ + (uint64_t)j * adj_every_;
+        scatter_dense(tb0_.as<uint32_t>());
+        for (int i = 0; i < k; ++i) {
+            StepArgs a = args(step_);
+            a.sample = 1;
+            a.tape_key = tkey_.as<uint32_t>() + (size_t)i * N_;
+            a.tape_lab = tlab_.as<uint32_t>() + (size_t)i * N_;
+            a.tape_ncell = tncell_.as<uint32_t>() + (size_t)i * cells_;
+            check(launch_step(a, params_.algorithm, false, pbuf_, grid_, stream_), "tape step");
+            check(launch_sample_finalize(samp_.as<float4>(), acc_.as<SampleAcc>(), cells_, 1, sms_ * 8, stream_,
+                                         tcnt_.as<uint32_t>() + (size_t)i * cells_),
+                  "tape sample");
+            ++step_;
+        }
+        last_step_table_ = false;
+        dense_valid_ = false;
+        return k;
+    }
+
     // Dense post-step arrays (dense_pos_, dense_vel_) -> buckets of step step_:
-    // the scatter plays the epilogue of step step_ - 1.
-    void scatter_dense()
+    // the scatter plays the epilogue of step step_ - 1 (tape_b0: bounce bits of its streaming).
+    void scatter_dense(uint32_t* tape_b0 = nullptr)
     {
         const uint64_t k = step_;
         for (uint64_t j = k; j < k + 2; ++j) {
@@ -608,6 +970,7 @@ private:
                   "clear overflow list");
         }
         StepArgs a = args(k - 1);   // out_* = buckets, counts and overflow list of step k
+        a.tape_lab = tape_b0;
         check(launch_scatter(a, dense_pos_.as<float>(), dense_vel_.as<float>(), N_, sms_ * 8, stream_),
               "scatter");
         dense_valid_ = true;
@@ -670,7 +1033,11 @@ private:
 
     static constexpr int kReduceBlocks = 1024;
 
-    mpcd_gb_params params_;
+    StepGraph graph_[2];                    // [sampling]
+    bool graphs_ = std::getenv("MPCD_GB_GRAPHS") == nullptr || std::getenv("MPCD_GB_GRAPHS")[0] != '0';
+    unsigned long long graph_base_host_ = 0;
+    mpcd_gb_params params_;                 // box 0 (algorithm and device of every box)
+    std::vector<mpcd_gb_params> box_params_;
     cudaStream_t own_stream_ = nullptr, stream_ = nullptr;
     int sms_ = 0, grid_ = 0;
     std::vector<BoxDesc> boxes_;
@@ -690,6 +1057,11 @@ private:
     DeviceBuffer boxes_d_, pos_[2], vel_[2], count_[3], ov_pos_[2], ov_vel_[2], state_, samp_, acc_, dense_pos_,
         dense_vel_, offsets_, scan_status_, scan_counter_, partial_;
     DeviceBuffer t_count_, t_gpos_, t_gvel_, t_axis_, t_gate_, t_gauss_;
+    // adjoint: checkpoints, tape of one segment, adjoint state
+    DeviceBuffer ckpt_, tkey_, tlab_, tncell_, tcnt_, tb0_, lam_, cellsum_, gsum_;
+    bool adj_valid_ = false;
+    uint64_t adj_s0_ = 0;
+    int adj_steps_ = 0, adj_every_ = 1;
 };
 
 }  // namespace mpcd_gb
@@ -731,16 +1103,22 @@ int32_t mpcd_gb_abi_version(void) { return MPCD_GB_ABI_VERSION; }
 
 int32_t mpcd_gb_create(const mpcd_gb_params* params, mpcd_gb_handle** out)
 {
+    return mpcd_gb_ensemble_create(params, 1, out);
+}
+
+int32_t mpcd_gb_ensemble_create(const mpcd_gb_params* params, int32_t R, mpcd_gb_handle** out)
+{
     g_create_error.clear();
-    if (!params || !out) {
-        g_create_error = "null argument";
+    if (!params || !out || R < 1) {
+        g_create_error = R < 1 ? "an ensemble needs at least one box" : "null argument";
+        if (out) *out = nullptr;
         return MPCD_GB_EINVAL;
     }
     *out = nullptr;
     auto* h = new (std::nothrow) mpcd_gb_handle;
     if (!h) return MPCD_GB_ENOMEM;
     try {
-        h->engine = new mpcd_gb::Engine(*params);
+        h->engine = new mpcd_gb::Engine(params, R);
     } catch (const mpcd_gb::Error& e) {
         g_create_error = e.what();
         delete h;
@@ -864,6 +1242,53 @@ int32_t mpcd_gb_counters(mpcd_gb_handle* h, uint64_t out[2])
 {
     if (!out) return MPCD_GB_EINVAL;
     return guarded(h, [&](mpcd_gb::Engine& e) { e.counters(out); });
+}
+
+int32_t mpcd_gb_set_particles_device(mpcd_gb_handle* h, const float* d_positions, const float* d_velocities)
+{
+    if (!d_positions && !d_velocities) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.set_device(d_positions, d_velocities); });
+}
+
+int32_t mpcd_gb_get_particles_device(mpcd_gb_handle* h, float* d_positions, float* d_velocities)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.get_device(d_positions, d_velocities); });
+}
+
+int32_t mpcd_gb_set_drag(mpcd_gb_handle* h, float drag)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.set_drag(drag); });
+}
+
+int32_t mpcd_gb_profile_forward(mpcd_gb_handle* h, int32_t steps, int32_t checkpoint_every, float* d_profile)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.profile_forward(steps, checkpoint_every, d_profile); });
+}
+
+int32_t mpcd_gb_profile_backward(mpcd_gb_handle* h, const float* d_grad_profile, float* d_grad_velocities,
+                                 double* grad_drag)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.profile_backward(d_grad_profile, d_grad_velocities, grad_drag); });
+}
+
+int32_t mpcd_gb_profile_tape(mpcd_gb_handle* h, uint32_t* key, uint32_t* lab, uint32_t* ncell, uint32_t* lab_count,
+                             uint32_t* bounce0)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.profile_tape(key, lab, ncell, lab_count, bounce0); });
+}
+
+int32_t mpcd_gb_num_boxes(const mpcd_gb_handle* h) { return h && h->engine ? h->engine->num_boxes() : 0; }
+
+int32_t mpcd_gb_box_range(mpcd_gb_handle* h, int32_t r, uint64_t out[4])
+{
+    if (!out) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.box_range(r, out); });
+}
+
+int32_t mpcd_gb_autotune(mpcd_gb_handle* h, int32_t steps_per_candidate, uint32_t out[2])
+{
+    if (!out) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.autotune(steps_per_candidate, out); });
 }
 
 int32_t mpcd_gb_cell_offsets_noalloc(mpcd_gb_handle* h, uint32_t* d_offsets, uint64_t n_offsets)

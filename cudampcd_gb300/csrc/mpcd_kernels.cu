@@ -175,25 +175,11 @@ __device__ __forceinline__ uint32_t claim_slot(uint32_t* count, uint32_t key, bo
     return slot;
 }
 
-// Accumulate (v, 1) into samp[lab] for every active lane, one atomic per distinct cell per warp.
+// Accumulate (v, 1) into samp[lab] for every active lane: one vector atomic
+// (red.global.add.v4.f32) per particle.
 __device__ __forceinline__ void sample_add(float4* samp, uint32_t lab, float3 v, bool active)
 {
-    unsigned todo = __ballot_sync(kFull, active);
-    while (todo) {
-        const int leader = __ffs(todo) - 1;
-        const uint32_t key = __shfl_sync(kFull, lab, leader);
-        const bool mine = active && ((todo >> (threadIdx.x & 31)) & 1u) && lab == key;
-        const unsigned grp = __ballot_sync(kFull, mine);
-        float sx = mine ? v.x : 0.0f, sy = mine ? v.y : 0.0f, sz = mine ? v.z : 0.0f;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            sx += __shfl_xor_sync(kFull, sx, o);
-            sy += __shfl_xor_sync(kFull, sy, o);
-            sz += __shfl_xor_sync(kFull, sz, o);
-        }
-        if ((int)(threadIdx.x & 31) == leader) atomicAdd(samp + key, make_float4(sx, sy, sz, (float)__popc(grp)));
-        todo &= ~grp;
-    }
+    if (active) atomicAdd(samp + lab, make_float4(v.x, v.y, v.z, 1.0f));
 }
 
 // Put one particle (already streamed and shifted for the next collision, in
@@ -221,6 +207,17 @@ __device__ __forceinline__ void store_particle(const StepArgs& a, const BoxDesc&
 }
 
 // ------------------------------------------------------------------ draws
+
+// SRD rotation axis of cell `ref` (box-local reference index) at `step`: uniform on the sphere.
+__device__ __forceinline__ float3 srd_axis_philox(const BoxDesc& b, uint64_t step, uint32_t ref)
+{
+    const uint4 o = draw(b, step, kAxis, ref, 0);
+    const float z = 1.0f - 2.0f * u01(o.x);
+    const float rho = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+    float s, c;
+    sincospif(2.0f * u01(o.y), &s, &c);
+    return make_float3(rho * c, rho * s, z);
+}
 
 template <bool TABLE>
 struct Draws;
@@ -254,12 +251,7 @@ struct Draws<false> {   // Philox (production)
     }
     __device__ static float3 srd_axis(const StepArgs&, const BoxDesc& b, uint64_t step, uint32_t ref)
     {
-        const uint4 o = draw(b, step, kAxis, ref, 0);
-        const float z = 1.0f - 2.0f * u01(o.x);
-        const float rho = sqrtf(fmaxf(0.0f, 1.0f - z * z));
-        float s, c;
-        sincospif(2.0f * u01(o.y), &s, &c);
-        return make_float3(rho * c, rho * s, z);
+        return srd_axis_philox(b, step, ref);
     }
     __device__ static float3 ext_axis(const StepArgs& a, const BoxDesc& b, uint64_t step, uint32_t ref, float& gate)
     {
@@ -423,7 +415,7 @@ __device__ __forceinline__ uint32_t fetch_count(const StepArgs& a, uint32_t tile
 // Overflow particles of step k (they found their bucket full when step k-1
 // scattered them): as in the reference, they skip the collision and keep the
 // unshifted position pbc(pbc(x + s) - s) (simulation_functions.cpp:90-93).
-__device__ void overflow_pass(const StepArgs& a)
+__device__ void overflow_pass(const StepArgs& a, uint64_t step)
 {
     const uint32_t n = min(a.state->ov_count[a.ov_in_slot], a.ov_cap);
     for (uint32_t base = 0; base < n; base += kThreads) {
@@ -437,7 +429,7 @@ __device__ void overflow_pass(const StepArgs& a)
             id = __float_as_uint(w.w);
             bi = box_of_particle(a.boxes, a.nboxes, id);
             const BoxDesc& b = a.boxes[bi];
-            const float3 s = grid_shift(b, bi, a.step, a.state);
+            const float3 s = grid_shift(b, bi, step, a.state);
             x = pbc(b, make_float3(p.x - s.x, p.y - s.y, p.z - s.z));   // post-step state
             v = make_float3(w.x, w.y, w.z);
             if (a.replay) {
@@ -446,8 +438,13 @@ __device__ void overflow_pass(const StepArgs& a)
                 a.dense_vel[i3] = v.x; a.dense_vel[i3 + 1] = v.y; a.dense_vel[i3 + 2] = v.z;
             } else {
                 vs = v;
-                xs = stream_shift(b, x, vs, grid_shift(b, bi, a.step + 1, a.state));
+                xs = stream_shift(b, x, vs, grid_shift(b, bi, step + 1, a.state));
                 key = b.cell_base + storage_index(b, cell_of(b, xs));
+                if (a.tape_key) {
+                    const bool bounced = vs.x != v.x || vs.y != v.y || vs.z != v.z;
+                    a.tape_key[id] = kTapeNone;
+                    a.tape_lab[id] = (b.cell_base + ref_index(b, cell_of(b, x))) | (bounced ? kTapeBounce : 0u);
+                }
             }
         }
         if (a.replay) continue;
@@ -495,10 +492,11 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
     }
     __syncthreads();
     uint32_t phase = 0;
+    const uint64_t step = a.step_base ? *a.step_base + a.step : a.step;   // graph replays read the base
 
     if (blockIdx.x == 0) {
         if (tid == 0 && !a.replay) a.state->ov_count[a.ov_zero_slot] = 0;   // list of step k-1, refilled by step k+1
-        overflow_pass(a);
+        overflow_pass(a, step);
     }
 
     // group of G threads per cell (every box of a launch has the same tile size)
@@ -514,8 +512,8 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
             if (bi != sbox_index) {   // box and its grid shifts change only between boxes
                 if (!SINGLE) sbox = *bp;
                 sbox_index = bi;
-                sshift[0] = grid_shift(*bp, bi, a.step, a.state);
-                sshift[1] = grid_shift(*bp, bi, a.step + 1, a.state);
+                sshift[0] = grid_shift(*bp, bi, step, a.state);
+                sshift[1] = grid_shift(*bp, bi, step + 1, a.state);
             }
         }
         __syncthreads();
@@ -539,10 +537,10 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                 if (ghosts) {
                     const uint32_t ref = ref_index(b, cc);
                     if (TABLE) {
-                        if (leader) gpart = D::ghost_count(a, b, a.step, ref, shift_abs, layer, sign);
+                        if (leader) gpart = D::ghost_count(a, b, step, ref, shift_abs, layer, sign);
                     } else {
                         for (uint32_t chunk = my_j; 4 * chunk < b.n; chunk += G) {   // 4 uniforms per Philox call
-                            const uint4 o = draw(b, a.step, kGhostCount, ref, chunk);
+                            const uint4 o = draw(b, step, kGhostCount, ref, chunk);
                             const uint32_t u[4] = {o.x, o.y, o.z, o.w};
 #pragma unroll
                             for (int k = 0; k < 4; ++k)
@@ -624,7 +622,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                     bool layer, ghosts;
                     wall_layer(b, cc.z, sign, layer, ghosts);
                     float3 gx, gv;
-                    D::ghost(a, b, a.step, ref_index(b, cc), j, cell_centre(b, cc), shift_abs, layer, sign, gx, gv);
+                    D::ghost(a, b, step, ref_index(b, cc), j, cell_centre(b, cc), shift_abs, layer, sign, gx, gv);
                     const uint32_t p = L.off[i] - pbase + L.cnt[i] + j;
                     s_pos[p] = make_float4(gx.x, gx.y, gx.z, 0.0f);
                     s_vel[p] = make_float4(gv.x, gv.y, gv.z, 0.0f);
@@ -685,10 +683,11 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                         const float inv = 1.0f / (float)n;
                         mean = make_float3((__ll2float_rn(sx) * 0x1p-32f) * inv, (__ll2float_rn(sy) * 0x1p-32f) * inv,
                                            (__ll2float_rn(sz) * 0x1p-32f) * inv);
-                        axis = D::srd_axis(a, b, a.step, ref_index(b, storage_coords(b, c0 + i)));
+                        axis = D::srd_axis(a, b, step, ref_index(b, storage_coords(b, c0 + i)));
                     }
                     L.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));
                     L.c1[i] = make_float4(axis.x, axis.y, axis.z, 0.0f);
+                    if (!REPLAY && a.tape_ncell) a.tape_ncell[b.cell_base + c0 + i] = n > 1 ? n : 0u;
                 }
             } else if (in_sub && leader) {
                 const uint32_t i = my_cell;
@@ -701,7 +700,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                 if (n > 1) {
                     const float3 centre = cell_centre(b, cc);
                     float gate;
-                    const float3 axis = D::ext_axis(a, b, a.step, ref, gate);
+                    const float3 axis = D::ext_axis(a, b, step, ref, gate);
                     auto at = [&](uint32_t k) -> uint32_t { return k < m ? s_inv[o + k] : o + cnt + (k - m); };
                     for (uint32_t k = 0; k < n; ++k) {
                         const uint32_t p = at(k);
@@ -743,7 +742,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                             const float3 x = make_float3(xp.x, xp.y, xp.z);
                             float3 v = make_float3(vp.x, vp.y, vp.z);
                             const bool side = dot3(x, axis) < 0;
-                            const float vr = D::thermal(a, b, a.step, ref, k) * b.tv;
+                            const float vr = D::thermal(a, b, step, ref, k) * b.tv;
                             if (side) mean0 += vr; else mean1 += vr;
                             const float3 cr = cross3(x, v);
                             dL.x += cr.x; dL.y += cr.y; dL.z += cr.z;
@@ -840,6 +839,12 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                         s_key[p] = b.cell_base + storage_index(b, cell_of(b, xn));
                         s_pos[p] = make_float4(xn.x, xn.y, xn.z, 0.0f);
                         s_vel[p] = make_float4(vn.x, vn.y, vn.z, vp.w);
+                        if (ALGO == 0 && a.tape_key) {
+                            const uint32_t id = __float_as_uint(vp.w);
+                            const bool bounced = vn.x != v.x || vn.y != v.y || vn.z != v.z;
+                            a.tape_key[id] = n > 1 ? b.cell_base + c0 + ci : kTapeNone;
+                            a.tape_lab[id] = (b.cell_base + ref_index(b, cell_of(b, x))) | (bounced ? kTapeBounce : 0u);
+                        }
                     }
                 } else if (p < np) {
                     s_key[p] = kNoKey;
@@ -901,6 +906,12 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
     }
 }
 
+// Advance the step base of graph replays by the steps one replay runs.
+__global__ void advance_kernel(DeviceState* state, unsigned steps)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) state->step_base += steps;
+}
+
 // ------------------------------------------------------------------ prologue scatter
 
 // Stream dense post-step particles for step k (a.step = k - 1: the launch plays
@@ -919,9 +930,11 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(StepArgs a, const flo
             bi = box_of_particle(a.boxes, a.nboxes, i);
             const BoxDesc& b = a.boxes[bi];
             vs = make_float3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+            const float3 v0 = vs;
             xs = stream_shift(b, make_float3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), vs,
                               grid_shift(b, bi, a.step + 1, a.state));
             key = b.cell_base + storage_index(b, cell_of(b, xs));
+            if (a.tape_lab) a.tape_lab[i] = (vs.x != v0.x || vs.y != v0.y || vs.z != v0.z) ? kTapeBounce : 0u;
         }
         store_particle(a, a.boxes[bi], xs, vs, (uint32_t)i, key, active);
     }
@@ -931,11 +944,13 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(StepArgs a, const flo
 
 // Per lab cell: mean velocity of the step (0 for an empty cell, as averageReduceOnly)
 // into the FP64 running sums; snapshot or accumulate (cpu_backend.cpp:189-211).
-__global__ void sample_finalize_kernel(float4* samp, SampleAcc* acc, uint64_t cells, int snapshot)
+__global__ void sample_finalize_kernel(float4* samp, SampleAcc* acc, uint64_t cells, int snapshot,
+                                       uint32_t* lab_count)
 {
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells;
          c += (uint64_t)gridDim.x * blockDim.x) {
         const float4 s = samp[c];
+        if (lab_count) lab_count[c] = (uint32_t)s.w;   // adjoint tape: particles sampled in the cell
         float mx = s.x, my = s.y, mz = s.z;
         if (s.w > 0.0f) {
             const float inv = 1.0f / s.w;
@@ -1154,6 +1169,105 @@ __global__ void subtract_kernel(float* vel, uint64_t begin, uint64_t end, float 
     }
 }
 
+// ------------------------------------------------------------------ adjoint of the sampled profile
+//
+// With the discrete events of a trajectory held fixed (collision cells and their
+// occupancy N_c incl. ghosts, grid shifts, rotation axes -- replayed from the
+// Philox counters --, bounce-backs, lab cells), the velocities are affine in the
+// initial velocities V0 and the body force g:
+//   P_0 = B_0 V0,  Q_t = Coll_t(P_t) (+ g dt e_x on collided particles),  P_{t+1} = B_{t+1} Q_t,
+//   Coll_t: v'_i = u_c + R_c (v_i - u_c),  u_c = (sum of the cell's particles and ghosts) / N_c,
+//   U(z) = sum_t sum_{x,y} m_c(t) / (S Lx Ly),  m_c(t) = sum_{i in lab cell c} Q_{t,i,x} / count_c(t),
+// where B flips the velocity of a bounced particle (simulation_functions.cpp:53-82) and
+// positions enter only through the fixed events.  Reverse sweep, t = S-1 .. 0:
+//   mu_t = B_{t+1} lambda_{t+1} + dU/dQ_t . dL/dU,
+//   lambda_{t,i} = R_c^T (mu_i - s_c) + s_c,  s_c = sum_{j in c} mu_j / N_c  (collided i; else mu_i),
+//   dL/dg += dt sum_{collided i} mu_{t,i,x},  and finally dL/dV0 = B_0 lambda_0.
+
+// U(z) of one box from the FP64 sample sums: one block per z layer.
+__global__ void __launch_bounds__(kThreads) profile_kernel(const SampleAcc* acc, BoxDesc b, double inv,
+                                                           float* profile)
+{
+    __shared__ double red[kThreads];
+    const uint32_t per = (uint32_t)(b.L[0] * b.L[1]);
+    double s = 0;
+    for (uint32_t k = threadIdx.x; k < per; k += kThreads) s += acc[b.cell_base + blockIdx.x * per + k].vx;
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = kThreads / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) profile[blockIdx.x] = (float)(red[0] * inv);
+}
+
+// mu = B_{t+1} lambda + sampling term; cell sums of mu over collided particles; dL/dg partial.
+__global__ void __launch_bounds__(kThreads) adjoint_pass1_kernel(BoxDesc b, uint32_t n, float* lam,
+                                                                 const uint32_t* key, const uint32_t* lab,
+                                                                 const uint32_t* lab_count, const float* dU,
+                                                                 double w, float4* cellsum, double* gsum)
+{
+    __shared__ double red[kThreads];
+    double gl = 0;
+    const uint32_t per = (uint32_t)(b.L[0] * b.L[1]);
+    for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+        float3 m = make_float3(lam[3 * i], lam[3 * i + 1], lam[3 * i + 2]);
+        const uint32_t l = lab[i];
+        if (l & kTapeBounce) m = make_float3(-m.x, -m.y, -m.z);
+        const uint32_t c = l & ~kTapeBounce;
+        const uint32_t z = (c - b.cell_base) / per;
+        m.x += (float)((double)dU[z] * w / (double)lab_count[c]);
+        lam[3 * i] = m.x; lam[3 * i + 1] = m.y; lam[3 * i + 2] = m.z;
+        const uint32_t k = key[i];
+        if (k != kTapeNone) {
+            atomicAdd(cellsum + k, make_float4(m.x, m.y, m.z, 0.0f));
+            gl += (double)m.x;
+        }
+    }
+    red[threadIdx.x] = gl;
+    __syncthreads();
+    for (int o = kThreads / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(gsum, red[0]);
+}
+
+// lambda = R^T (mu - s_c) + s_c for collided particles (R^T: rotation by -alpha).
+__global__ void __launch_bounds__(kThreads) adjoint_pass2_kernel(BoxDesc b, uint64_t step, uint32_t n, float* lam,
+                                                                 const uint32_t* key, const uint32_t* ncell,
+                                                                 const float4* cellsum)
+{
+    for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+        const uint32_t k = key[i];
+        if (k == kTapeNone) continue;
+        const float inv = 1.0f / (float)ncell[k];
+        const float4 cs = cellsum[k];
+        const float3 sc = make_float3(cs.x * inv, cs.y * inv, cs.z * inv);
+        const float3 a = srd_axis_philox(b, step, ref_index(b, storage_coords(b, k - b.cell_base)));
+        const float3 wv = make_float3(lam[3 * i] - sc.x, lam[3 * i + 1] - sc.y, lam[3 * i + 2] - sc.z);
+        const float d = dot3(wv, a);
+        const float3 para = make_float3(a.x * d, a.y * d, a.z * d);
+        const float3 perp = make_float3(wv.x - para.x, wv.y - para.y, wv.z - para.z);
+        const float3 cr = cross3(wv, a);
+        lam[3 * i] = (para.x + b.cos_a * perp.x) - b.sin_a * cr.x + sc.x;
+        lam[3 * i + 1] = (para.y + b.cos_a * perp.y) - b.sin_a * cr.y + sc.y;
+        lam[3 * i + 2] = (para.z + b.cos_a * perp.z) - b.sin_a * cr.z + sc.z;
+    }
+}
+
+// dL/dV0 = B_0 lambda_0.
+__global__ void __launch_bounds__(kThreads) adjoint_finish_kernel(uint32_t n, const float* lam, const uint32_t* b0,
+                                                                  float* out)
+{
+    for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+        const float f = (b0[i] & kTapeBounce) ? -1.0f : 1.0f;
+        out[3 * i] = f * lam[3 * i];
+        out[3 * i + 1] = f * lam[3 * i + 1];
+        out[3 * i + 2] = f * lam[3 * i + 2];
+    }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
@@ -1193,8 +1307,45 @@ cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* bl
                                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
                     if (e != cudaSuccess) return e;
                 }
+    // load the kernels that step graphs capture before any capture begins
+    cudaFuncAttributes attr;
+    cudaError_t e = cudaFuncGetAttributes(&attr, (const void*)advance_kernel);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, (const void*)sample_finalize_kernel);
+    if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         blocks_per_sm, (const void*)kStepFns[algorithm ? 1 : 0][0][1][0], kThreads, smem);
+}
+
+cudaError_t launch_profile(const SampleAcc* acc, const BoxDesc& b, uint64_t samples, float* profile, cudaStream_t st)
+{
+    const double inv = 1.0 / ((double)samples * (double)b.L[0] * (double)b.L[1]);
+    profile_kernel<<<(unsigned)b.L[2], kThreads, 0, st>>>(acc, b, inv, profile);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_step(const BoxDesc& b, uint64_t step, uint64_t samples, float* lam, const uint32_t* key,
+                                const uint32_t* lab, const uint32_t* ncell, const uint32_t* lab_count,
+                                const float* dU, float4* cellsum, double* gsum, int grid, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(cellsum, 0, sizeof(float4) * b.C, st);
+    if (e != cudaSuccess) return e;
+    const double w = 1.0 / ((double)samples * (double)b.L[0] * (double)b.L[1]);
+    adjoint_pass1_kernel<<<grid, kThreads, 0, st>>>(b, b.N, lam, key, lab, lab_count, dU, w, cellsum, gsum);
+    adjoint_pass2_kernel<<<grid, kThreads, 0, st>>>(b, step, b.N, lam, key, ncell, cellsum);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_finish(uint32_t n, const float* lam, const uint32_t* b0, float* out, int grid,
+                                  cudaStream_t st)
+{
+    adjoint_finish_kernel<<<grid, kThreads, 0, st>>>(n, lam, b0, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advance(DeviceState* state, unsigned steps, cudaStream_t st)
+{
+    advance_kernel<<<1, 32, 0, st>>>(state, steps);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel, uint64_t n_total, int grid,
@@ -1205,9 +1356,9 @@ cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel
 }
 
 cudaError_t launch_sample_finalize(float4* samp, SampleAcc* acc, uint64_t cells, int snapshot, int grid,
-                                   cudaStream_t st)
+                                   cudaStream_t st, uint32_t* lab_count)
 {
-    sample_finalize_kernel<<<grid, kThreads, 0, st>>>(samp, acc, cells, snapshot);
+    sample_finalize_kernel<<<grid, kThreads, 0, st>>>(samp, acc, cells, snapshot, lab_count);
     return cudaGetLastError();
 }
 

@@ -16,12 +16,23 @@ size_t step_smem_bytes(uint32_t pbuf, uint32_t cells, int algorithm);
 cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* blocks_per_sm);
 // One step of every box (algorithm 0 = SRD, 1 = extended; table = injected draws).
 cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st);
+// state->step_base += steps (the last node of a replayed step graph).
+cudaError_t launch_advance(DeviceState* state, unsigned steps, cudaStream_t st);
 // Key dense clean particles for step a.step + 1 and scatter them into a.out_*.
 cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel, uint64_t n_total, int grid,
                            cudaStream_t st);
 // Lab-grid sample of one step into the FP64 running sums (and clear the step sums).
 cudaError_t launch_sample_finalize(float4* samp, SampleAcc* acc, uint64_t cells, int snapshot, int grid,
-                                   cudaStream_t st);
+                                   cudaStream_t st, uint32_t* lab_count = nullptr);
+// Adjoint of the sampled x-velocity profile (single box, SRD): U(z) from the sample
+// sums of `samples` steps; one reverse step (both passes) at absolute step `step`;
+// dL/dV0 from the final adjoint and the bounce bits of the initial streaming.
+cudaError_t launch_profile(const SampleAcc* acc, const BoxDesc& b, uint64_t samples, float* profile, cudaStream_t st);
+cudaError_t launch_adjoint_step(const BoxDesc& b, uint64_t step, uint64_t samples, float* lam, const uint32_t* key,
+                                const uint32_t* lab, const uint32_t* ncell, const uint32_t* lab_count,
+                                const float* dU, float4* cellsum, double* gsum, int grid, cudaStream_t st);
+cudaError_t launch_adjoint_finish(uint32_t n, const float* lam, const uint32_t* b0, float* out, int grid,
+                                  cudaStream_t st);
 // Layout dump: cells in storage order, stable order within a cell (decoupled
 // look-back scan of the counts, then one thread per cell), then the overflow
 // list.  offsets: cells + 1 entries.

@@ -60,6 +60,7 @@ struct DeviceState {
     unsigned long long inject_step[kMaxInjectedShifts];
     float inject_shift[kMaxInjectedShifts][4];
     unsigned int inject_valid[kMaxInjectedShifts];
+    unsigned long long step_base;        // graph replays: absolute step of the replay's first step
 };
 
 enum : unsigned int {
@@ -86,7 +87,8 @@ struct StepArgs {
     uint32_t boxes_tile_cells;    // cells per tile (the same for every box of a launch)
     uint32_t num_tiles;
     uint64_t total_slots;
-    uint64_t step;                // k: this launch completes step k
+    uint64_t step;                // k: this launch completes step k (step_base: k - *step_base)
+    const unsigned long long* step_base;   // non-null in graph replays: k = *step_base + step
     // buckets holding the particles entering collision k (streamed, shifted)
     const float4* in_pos;
     const float4* in_vel;
@@ -113,6 +115,19 @@ struct StepArgs {
     float4* samp;                 // [global cells] (sum vx, vy, vz, count)
     float ext_axis[13][3];        // discrete axis set of the extended collision
     DrawTables draws;             // used by the injected-draw instantiation
+    // adjoint tape of this step, by particle id / cell (null: not recorded):
+    //   tape_key[id]  = collision cell (global storage index) if the particle was
+    //                   collided (cell with n > 1), else kTapeNone;
+    //   tape_lab[id]  = lab cell it was sampled in (global, reference order) |
+    //                   kTapeBounce if the streaming that follows bounced it;
+    //   tape_ncell[c] = particles incl. ghosts of collided cell c (storage index).
+    // The scatter records only the bounce bit of its streaming in tape_lab.
+    uint32_t* tape_key;
+    uint32_t* tape_lab;
+    uint32_t* tape_ncell;
 };
+
+constexpr uint32_t kTapeNone = 0xFFFFFFFFu;
+constexpr uint32_t kTapeBounce = 0x80000000u;
 
 }  // namespace mpcd_gb

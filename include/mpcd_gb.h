@@ -150,6 +150,62 @@ int32_t mpcd_gb_inject_draws(mpcd_gb_handle *h, uint32_t gmax, uint32_t pmax, co
  * [1] error flags (bit 0 overflow list full, bit 1 wait timeout, bit 2 key mismatch). */
 int32_t mpcd_gb_counters(mpcd_gb_handle *h, uint64_t out[2]);
 
+/* ---- batched ensemble (no counterpart in the reference) ---- */
+
+/* R independent boxes advanced together: one step-kernel launch per step walks a
+ * table of boxes (per-box geometry, n, drag, temperature, time step and Philox seed;
+ * every box must use the same algorithm and device).  Box r evolves exactly as a
+ * single-box handle created from params[r] does.  On an ensemble handle:
+ * mpcd_gb_num_particles / mpcd_gb_num_cells are totals; the getters, setters and
+ * mpcd_gb_get_sample_mean concatenate the boxes in order (particles of box r at
+ * [first_particle, +num_particles), cells of box r at [first_cell, +num_cells) in
+ * that box's own x + Lx*(y + Ly*z) order); mpcd_gb_inject_shift applies to box 0 and
+ * mpcd_gb_inject_draws needs R = 1.  mpcd_gb_create(p, h) is the R = 1 case. */
+int32_t mpcd_gb_ensemble_create(const mpcd_gb_params *params, int32_t R, mpcd_gb_handle **out);
+/* Number of boxes of the handle. */
+int32_t mpcd_gb_num_boxes(const mpcd_gb_handle *h);
+/* out = {first_particle, num_particles, first_cell, num_cells} of box r. */
+int32_t mpcd_gb_box_range(mpcd_gb_handle *h, int32_t r, uint64_t out[4]);
+/* Choose the tile size (cells per tile, a power of two in 8..128) and the particle
+ * buffer of the step kernel by timing steps_per_candidate real steps of every
+ * admissible pair (the steps advance the simulation); out = {tile cells, buffer}. */
+int32_t mpcd_gb_autotune(mpcd_gb_handle *h, int32_t steps_per_candidate, uint32_t out[2]);
+
+/* ---- device-pointer I/O and the differentiable channel (no counterpart in the reference) ---- */
+
+/* As mpcd_gb_set_particles / the getters, with device buffers of 3N floats (either may be
+ * NULL to keep or skip that array). */
+int32_t mpcd_gb_set_particles_device(mpcd_gb_handle *h, const float *d_positions, const float *d_velocities);
+int32_t mpcd_gb_get_particles_device(mpcd_gb_handle *h, float *d_positions, float *d_velocities);
+
+/* Body force (SimulationParameters::drag) of every box from the next step on. */
+int32_t mpcd_gb_set_drag(mpcd_gb_handle *h, float drag);
+
+/* Sampled x-velocity profile of a single-box SRD handle, and its adjoint.
+ * Forward: from the current state, run `steps` steps sampling each one, checkpoint the
+ * particle state every `checkpoint_every` steps, and write
+ *   U[z] = (1 / (steps Lx Ly)) sum_t sum_{x,y} mean v_x of lab cell (x, y, z) at step t
+ * (d_profile: device float[Lz], Lz of the container).  The sample sums of the handle
+ * are overwritten.
+ * Backward: given d_grad_profile = dL/dU (device float[Lz]), write dL/dV0 (device
+ * float[3N], V0 = the velocities at the start of the forward, by particle id) and
+ * dL/d(drag) (host double).  Collision cells, grid shifts, rotation axes, ghost counts
+ * and wall bounces are held fixed at those of the forward trajectory: each checkpoint
+ * segment is recomputed (its draws replayed from the Philox counters) and then swept
+ * in reverse.  Afterwards the handle's particle state is that of an intermediate step;
+ * set the particles again before stepping on. */
+int32_t mpcd_gb_profile_forward(mpcd_gb_handle *h, int32_t steps, int32_t checkpoint_every, float *d_profile);
+int32_t mpcd_gb_profile_backward(mpcd_gb_handle *h, const float *d_grad_profile, float *d_grad_velocities,
+                                 double *grad_drag);
+/* Test hook: the fixed events of every step of the last profile forward, host arrays:
+ * key[steps*N] (collision cell, storage order, or 0xFFFFFFFF if not collided),
+ * lab[steps*N] (lab cell, reference order, | 0x80000000 if the streaming after that
+ * step bounced the particle), ncell[steps*C] (particles + ghosts of each collided cell,
+ * storage order), lab_count[steps*C], bounce0[N] (0x80000000 if the streaming into the
+ * first step bounced the particle).  Any pointer may be NULL. */
+int32_t mpcd_gb_profile_tape(mpcd_gb_handle *h, uint32_t *key, uint32_t *lab, uint32_t *ncell, uint32_t *lab_count,
+                             uint32_t *bounce0);
+
 /* ---- allocation-free cell offsets (no counterpart in the reference) ---- */
 
 /* Largest cell count (C) that mpcd_gb_cell_offsets_noalloc accepts. */
