@@ -8,6 +8,19 @@ benchmark (benchmark.py:36-47).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
+Batched ensemble: --ensemble R runs R independent channel replicas drawn from a
+seeded generator (Lx, Ly in {8, 16, 32, 64}, Lz uniform in [20, 200] incl. walls,
+n in {5, 10, 20}, drag log-uniform in [1e-4, 1e-2], T = 1, dt = 0.02, seed
+base + r) in one handle -- one step-kernel launch per step, CUDA-graph replays,
+autotuned tiles -- and the same replicas stepped one handle at a time, and
+prints one line with both rates.
+
+Physics: --physics extended runs the extended-MPC channel with the non-ideal
+equation of state (256 x 256 x 64 cells + 2 walls, n = 20, T = 1, dt = 0.02,
+g = 0.0005): warm-up, then the wall pressure, the density profile and the
+viscosity from the curvature of the sampled velocity profile.  --physics srd
+runs the same measurement with the SRD collision.
+
 Profiling options (the default run uses none of them): --size LX LY LZ replaces
 the fluid cells of the workload (walls are added in z), --algorithm extended
 switches the collision, --no-e2e and --no-cpu skip those parts.
@@ -296,6 +309,111 @@ def run_gpu_arm(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+def ensemble_boxes(R: int, seed: int = 0):
+    """The replicas of the batched workload (numpy default_rng(seed))."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    boxes = []
+    for r in range(R):
+        lx, ly = (int(v) for v in rng.choice([8, 16, 32, 64], size=2))
+        lz = int(rng.integers(20, 201))
+        n = int(rng.choice([5, 10, 20]))
+        drag = float(10 ** rng.uniform(-4, -2))
+        boxes.append(dict(L=(lx, ly, lz), periodic=(1, 1, 0), n=n, dt=0.02, drag=drag, temperature=1.0,
+                          seed=1000 + r))
+    return boxes
+
+
+def run_ensemble(args):
+    import torch
+
+    from cudampcd_gb300 import capi
+
+    boxes = ensemble_boxes(args.ensemble)
+    K = args.steps
+    h = capi.Handle(boxes=boxes)
+    N = h.N
+    tile_cells, pbuf = h.autotune(2)
+    h.step(max(args.warmup, 6))
+    h.synchronize()
+    with ClockSampler(0) as clocks:
+        t0 = time.perf_counter()
+        h.step(K)
+        h.synchronize()
+        t_batched = time.perf_counter() - t0
+    flags = h.counters()[1]
+    h.close()
+    torch.cuda.synchronize()
+    t_seq = 0.0
+    for b in boxes:   # the same replicas through the plain single-box path, one after the other
+        s = capi.Handle(**b)
+        s.step(6)
+        s.synchronize()
+        t0 = time.perf_counter()
+        s.step(K)
+        s.synchronize()
+        t_seq += time.perf_counter() - t0
+        s.close()
+    batched, sequential = N * K / t_batched, N * K / t_seq
+    out = {"metric": METRIC, "value": batched, "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": args.warmup,
+           "ms_per_step": 1e3 * t_batched / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"batched SRD ensemble: {len(boxes)} channel replicas, N = {N}, "
+                                  "Lx,Ly in {8,16,32,64}, Lz in [20,200], n in {5,10,20}, drag log-uniform "
+                                  "[1e-4,1e-2], T=1, dt=0.02, seeds 1000+r (numpy default_rng(0))",
+                      "tiles": {"cells_per_tile": tile_cells, "particle_buffer": pbuf},
+                      "timing": "host wall clock around step(K) + synchronize, both arms"},
+           "batched_vs_sequential": {"batched": batched, "sequential": sequential, "speedup": batched / sequential},
+           "clocks": clocks.summary(), "device_counters": {"error_flags": flags}}
+    print(json.dumps(out), flush=True)
+
+
+def run_physics(args):
+    import numpy as np
+
+    from cudampcd_gb300 import capi
+
+    alg = 1 if args.physics == "extended" else 0
+    Lx, Ly, Lz = (args.size or (256, 256, 64))
+    n, g, dt = 20, 0.0005, 0.02
+    h = capi.Handle(L=(Lx, Ly, Lz + 2), periodic=(1, 1, 0), n=n, dt=dt, drag=g, algorithm=alg, seed=0)
+    t0 = time.perf_counter()
+    h.step(args.warmup)
+    h.synchronize()
+    t_warm = time.perf_counter() - t0
+    blocks, per = 8, max(1, args.steps // 8)
+    etas, P = [], []
+    zc = np.arange(Lz + 2) + 0.5 - (Lz + 2) / 2.0
+    fluid = slice(1, Lz + 1)
+    A = np.stack([np.ones(Lz), -(zc[fluid] ** 2 + 1.0 / 12.0)], axis=1)
+    dens = np.zeros(Lz + 2)
+    for _ in range(blocks):
+        h.wall_pressure(restart=True)
+        h.step_and_sample(per)
+        p0, p1, _ = h.wall_pressure()
+        P.append((p0 + p1) / 2)
+        d, v = h.sample_mean()
+        u = v[:, 0].reshape(Lz + 2, Ly, Lx).mean(axis=(1, 2)) * (per - 1) / per
+        dens += d.reshape(Lz + 2, Ly, Lx).mean(axis=(1, 2)) * (per - 1) / per / blocks
+        (a, b), *_ = np.linalg.lstsq(A, u[fluid], rcond=None)
+        etas.append(n * g / (2.0 * b))
+    etas, P = np.array(etas), np.array(P)
+    srd_theory = (1 - np.cos(2 * np.pi / 3)) / (18 * dt) * (n - 1 + np.exp(-n))
+    out = {"physics": args.physics, "workload": f"{args.physics} channel {Lx}x{Ly}x{Lz} cells + 2 walls, n={n}, "
+                                                f"T=1, dt={dt}, g={g}, N={h.N}",
+           "warmup_steps": args.warmup, "sampled_steps": blocks * per, "warmup_s": t_warm,
+           "wall_pressure": {"mean": float(P.mean()), "stderr": float(P.std(ddof=1) / np.sqrt(blocks)),
+                             "ideal_gas_nT": float(n)},
+           "viscosity": {"mean": float(etas.mean()), "stderr": float(etas.std(ddof=1) / np.sqrt(blocks)),
+                         "srd_theory": float(srd_theory), "blocks": [float(e) for e in etas]},
+           "density_profile_fluid": {"mean": float(dens[fluid].mean()), "min": float(dens[fluid].min()),
+                                     "max": float(dens[fluid].max()), "first_layers": [float(x) for x in dens[1:5]]},
+           "device_counters": {"bucket_overflows": h.counters()[0], "error_flags": h.counters()[1]}}
+    h.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -307,13 +425,19 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--size", type=int, nargs=3, metavar=("LX", "LY", "LZ"))
     ap.add_argument("--algorithm", default="srd", choices=["srd", "extended"])
+    ap.add_argument("--ensemble", type=int, default=0, metavar="R")
+    ap.add_argument("--physics", choices=["extended", "srd"])
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
-    if args.impl == "reference":
+    if args.ensemble:
+        run_ensemble(args)
+    elif args.physics:
+        run_physics(args)
+    elif args.impl == "reference":
         run_reference_arm(args, rank)
     else:
         run_gpu_arm(args, rank, world, local_rank)

@@ -77,6 +77,8 @@ def lib() -> C.CDLL:
         L.mpcd_gb_set_particles_device.argtypes = [H, C.c_void_p, C.c_void_p]
         L.mpcd_gb_get_particles_device.argtypes = [H, C.c_void_p, C.c_void_p]
         L.mpcd_gb_set_drag.argtypes = [H, C.c_float]
+        L.mpcd_gb_set_step.argtypes = [H, C.c_uint64]
+        L.mpcd_gb_wall_pressure.argtypes = [H, C.c_int32, np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")]
         L.mpcd_gb_profile_forward.argtypes = [H, C.c_int32, C.c_int32, C.c_void_p]
         L.mpcd_gb_profile_backward.argtypes = [H, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
         L.mpcd_gb_profile_tape.argtypes = [H] + [C.c_void_p] * 5
@@ -235,6 +237,15 @@ class Handle:
     def get_particles_device(self, d_pos, d_vel):
         self._check(self._lib.mpcd_gb_get_particles_device(self.h, C.c_void_p(d_pos or None),
                                                            C.c_void_p(d_vel or None)))
+
+    def set_step(self, step):
+        self._check(self._lib.mpcd_gb_set_step(self.h, int(step)))
+
+    def wall_pressure(self, restart=False):
+        """(bottom, top) wall pressure over the steps since the last restart, and that step count."""
+        out = np.zeros(3, np.float64)
+        self._check(self._lib.mpcd_gb_wall_pressure(self.h, 1 if restart else 0, out))
+        return float(out[0]), float(out[1]), int(out[2])
 
     def set_drag(self, drag):
         self._check(self._lib.mpcd_gb_set_drag(self.h, float(drag)))

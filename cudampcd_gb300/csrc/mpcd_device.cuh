@@ -71,25 +71,28 @@ __device__ __forceinline__ float3 grid_shift(const BoxDesc& b, int box_index, ui
 // For a = r + 1.5L in [0, 3L) the remainder is a - qL with q in {0,1,2}, and
 // that difference is exact (Sterbenz), i.e. identical to fmodf.  The common
 // case is evaluated branch-free; arguments outside [0, 3L) take fmodf itself.
-__device__ __forceinline__ float pbc1(float r, float L)
+// L15 = 1.5f * L, L2 = 2.0f * L, L3 = 3.0f * L, Lh = L * 0.5f (exact float products).
+__device__ __forceinline__ float pbc1(float r, float L, float L15, float L2, float L3, float Lh)
 {
-    const float a = r + 1.5f * L;
-    const float q = a >= 2.0f * L ? 2.0f * L : (a >= L ? L : 0.0f);
+    const float a = r + L15;
+    const float q = a >= L2 ? L2 : (a >= L ? L : 0.0f);
     float m = a - q;
-    if (__builtin_expect(!(a >= 0.0f && a < 3.0f * L), 0)) m = fmodf(a, L);
-    return m - L * 0.5f;
+    if (__builtin_expect(!(a >= 0.0f && a < L3), 0)) m = fmodf(a, L);
+    return m - Lh;
 }
 
 __device__ __forceinline__ float3 pbc(const BoxDesc& b, float3 r)
 {
-    return make_float3(pbc1(r.x, b.Lf[0]), pbc1(r.y, b.Lf[1]), pbc1(r.z, b.Lf[2]));
+    return make_float3(pbc1(r.x, b.Lf[0], b.L15[0], b.L2x[0], b.L3x[0], b.Lh[0]),
+                       pbc1(r.y, b.Lf[1], b.L15[1], b.L2x[1], b.L3x[1], b.Lh[1]),
+                       pbc1(r.z, b.Lf[2], b.L15[2], b.L2x[2], b.L3x[2], b.Lh[2]));
 }
 
 // Coordinate of a cell along one axis: floor(x + L/2) mod L, with the
 // float -> uint32 conversion of the reference's x86-64 build (via int64).
-__device__ __forceinline__ uint32_t cell_coord(float x, float Lf, uint32_t L)
+__device__ __forceinline__ uint32_t cell_coord(float x, float Lf, float Lh, uint32_t L)
 {
-    const float f = floorf(x + Lf * 0.5f);
+    const float f = floorf(x + Lh);
     uint32_t c = (uint32_t)(int)f;
     c = c == L ? 0u : c;
     if (__builtin_expect(!(f >= 0.0f && f <= Lf), 0)) c = (uint32_t)(long long)f % L;
@@ -98,8 +101,9 @@ __device__ __forceinline__ uint32_t cell_coord(float x, float Lf, uint32_t L)
 
 __device__ __forceinline__ uint3 cell_of(const BoxDesc& b, float3 x)
 {
-    return make_uint3(cell_coord(x.x, b.Lf[0], (uint32_t)b.L[0]), cell_coord(x.y, b.Lf[1], (uint32_t)b.L[1]),
-                      cell_coord(x.z, b.Lf[2], (uint32_t)b.L[2]));
+    return make_uint3(cell_coord(x.x, b.Lf[0], b.Lh[0], (uint32_t)b.L[0]),
+                      cell_coord(x.y, b.Lf[1], b.Lh[1], (uint32_t)b.L[1]),
+                      cell_coord(x.z, b.Lf[2], b.Lh[2], (uint32_t)b.L[2]));
 }
 
 // reference cell index x + Lx*(y + Ly*z) (volume_container.hpp:330-336)
@@ -132,8 +136,7 @@ __device__ __forceinline__ uint3 storage_coords(const BoxDesc& b, uint32_t s)
 // centre of a cell in the shifted frame (volume_container.hpp:347-352)
 __device__ __forceinline__ float3 cell_centre(const BoxDesc& b, uint3 c)
 {
-    return make_float3((0.5f + (float)c.x) - b.Lf[0] * 0.5f, (0.5f + (float)c.y) - b.Lf[1] * 0.5f,
-                       (0.5f + (float)c.z) - b.Lf[2] * 0.5f);
+    return make_float3((0.5f + (float)c.x) - b.Lh[0], (0.5f + (float)c.y) - b.Lh[1], (0.5f + (float)c.z) - b.Lh[2]);
 }
 
 // Streaming with bounce-back (simulation_functions.cpp:53-82), in place.
@@ -142,7 +145,7 @@ __device__ __forceinline__ void stream(const BoxDesc& b, float3& x, float3& v)
     const float dt = b.dt;
     if (!b.channel) {
         if (b.wall_z) {
-            const float z_wall = (0.5f * b.Lf[2] - 1);
+            const float z_wall = (b.Lh[2] - 1);   // 0.5f * Lz - 1
             const float next_z = x.z + v.z * dt;
             if (fabsf(next_z) > z_wall) {
                 const float time_left = (next_z > 0 ? z_wall - x.z : -z_wall - x.z) / v.z;

@@ -255,6 +255,45 @@ public:
         check(cudaStreamSynchronize(stream_), "particle read");
     }
 
+    // Continue from the current particle state with the step counter (the key
+    // of every Philox draw) set to k.
+    void set_step(uint64_t k)
+    {
+        if (k >= (1ull << 40)) throw Error(MPCD_GB_EINVAL, "step index beyond 2^40");
+        materialise();
+        step_ = k;
+        scatter_dense();
+        check_device_errors();
+        sampling_ = false;
+    }
+
+    // Wall pressure estimator: restart zeroes the impulse sums and measures every
+    // step from now on; out = {bottom, top} pressure and the steps measured.
+    void wall_pressure(bool restart, double out[3])
+    {
+        if (boxes_.size() != 1 || !boxes_[0].wall_z)
+            throw Error(MPCD_GB_ESTATE, "the wall pressure needs a single box with walls in z");
+        const size_t off = offsetof(DeviceState, wall_impulse);
+        if (restart) {
+            check(cudaMemsetAsync(static_cast<char*>(state_.p) + off, 0, 2 * sizeof(double), stream_), "pressure");
+            if (!pressure_) {
+                pressure_ = true;
+                for (auto& g : graph_) g.reset();   // the graphs bake the flag into their launches
+            }
+            pressure_step0_ = step_;
+        }
+        double imp[2] = {0, 0};
+        check(cudaMemcpyAsync(imp, static_cast<char*>(state_.p) + off, sizeof imp, cudaMemcpyDeviceToHost, stream_),
+              "pressure");
+        check(cudaStreamSynchronize(stream_), "pressure");
+        const BoxDesc& b = boxes_[0];
+        const double steps = (double)(step_ - pressure_step0_);
+        const double norm = steps > 0 ? 1.0 / ((double)b.L[0] * b.L[1] * steps * b.dt) : 0.0;
+        out[0] = imp[0] * norm;
+        out[1] = imp[1] * norm;
+        out[2] = steps;
+    }
+
     // Body force of every box from the next step on.
     void set_drag(float drag)
     {
@@ -605,6 +644,10 @@ private:
         for (int d = 0; d < 3; ++d) {
             b.L[d] = (int32_t)p.volume_size[d];
             b.Lf[d] = p.volume_size[d];
+            b.L15[d] = 1.5f * b.Lf[d];
+            b.L2x[d] = 2.0f * b.Lf[d];
+            b.L3x[d] = 3.0f * b.Lf[d];
+            b.Lh[d] = b.Lf[d] * 0.5f;
             b.periodic[d] = p.periodicity[d];
             Nf *= (uint64_t)(b.L[d] - 2 * (1 - b.periodic[d]));
         }
@@ -817,6 +860,7 @@ private:
         a.replay = replay ? 1 : 0;
         a.dense_pos = dense_pos_.as<float>();
         a.dense_vel = dense_vel_.as<float>();
+        a.pressure = pressure_ && !replay ? 1 : 0;
         return a;
     }
 
@@ -1060,6 +1104,8 @@ private:
     // adjoint: checkpoints, tape of one segment, adjoint state
     DeviceBuffer ckpt_, tkey_, tlab_, tncell_, tcnt_, tb0_, lam_, cellsum_, gsum_;
     bool adj_valid_ = false;
+    bool pressure_ = false;
+    uint64_t pressure_step0_ = 0;
     uint64_t adj_s0_ = 0;
     int adj_steps_ = 0, adj_every_ = 1;
 };
@@ -1253,6 +1299,17 @@ int32_t mpcd_gb_set_particles_device(mpcd_gb_handle* h, const float* d_positions
 int32_t mpcd_gb_get_particles_device(mpcd_gb_handle* h, float* d_positions, float* d_velocities)
 {
     return guarded(h, [&](mpcd_gb::Engine& e) { e.get_device(d_positions, d_velocities); });
+}
+
+int32_t mpcd_gb_set_step(mpcd_gb_handle* h, uint64_t step)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.set_step(step); });
+}
+
+int32_t mpcd_gb_wall_pressure(mpcd_gb_handle* h, int32_t restart, double out[3])
+{
+    if (!out) return MPCD_GB_EINVAL;
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.wall_pressure(restart != 0, out); });
 }
 
 int32_t mpcd_gb_set_drag(mpcd_gb_handle* h, float drag)

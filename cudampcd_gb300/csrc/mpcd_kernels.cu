@@ -347,6 +347,7 @@ __device__ __forceinline__ void sym_inverse(const float m[6], float tol, float o
 // order, as the reference walks it in index order.
 
 constexpr uint32_t kNoKey = 0xFFFFFFFFu;
+constexpr uint32_t kGhostFlag = 0x8000u;   // s_cell entries of ghost particles (tile cells < 2^15)
 constexpr int kMaxPerThread = 8;   // particle buffer <= kMaxPerThread * kThreads
 
 // Shared memory of one CTA, carved from the dynamic allocation:
@@ -400,11 +401,12 @@ __device__ inline TileLayout carve(unsigned char* base, uint32_t pbuf, uint32_t 
 // Count of cell `c` of `tile` (first thread of the cell's group); issued one
 // tile ahead so its latency hides.  Outside a replay it also clears the same
 // cell of the counts of step k-1, which step k+1 will fill.
+template <bool SINGLE>
 __device__ __forceinline__ uint32_t fetch_count(const StepArgs& a, uint32_t tile, uint32_t c, bool leader)
 {
     if (!leader || tile >= a.num_tiles) return 0;
-    int bi;
-    const BoxDesc* bp = find_box(a, tile, bi);
+    int bi = 0;
+    const BoxDesc* bp = SINGLE ? &a.box0 : find_box(a, tile, bi);
     const uint32_t c0 = (tile - bp->tile_base) * bp->tile_cells;
     if (c >= min(bp->tile_cells, bp->C - c0)) return 0;
     const uint32_t g = bp->cell_base + c0 + c;
@@ -440,6 +442,8 @@ __device__ void overflow_pass(const StepArgs& a, uint64_t step)
                 vs = v;
                 xs = stream_shift(b, x, vs, grid_shift(b, bi, step + 1, a.state));
                 key = b.cell_base + storage_index(b, cell_of(b, xs));
+                if (a.pressure && b.wall_z && vs.z != v.z)   // bounce-back: 2 |v_z| outward
+                    atomicAdd(&a.state->wall_impulse[v.z > 0.0f ? 1 : 0], 2.0 * fabs((double)v.z));
                 if (a.tape_key) {
                     const bool bounced = vs.x != v.x || vs.y != v.y || vs.z != v.z;
                     a.tape_key[id] = kTapeNone;
@@ -493,6 +497,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
     __syncthreads();
     uint32_t phase = 0;
     const uint64_t step = a.step_base ? *a.step_base + a.step : a.step;   // graph replays read the base
+    float imp[2] = {0.0f, 0.0f};   // pressure estimator: this thread's outward wall impulses
 
     if (blockIdx.x == 0) {
         if (tid == 0 && !a.replay) a.state->ov_count[a.ov_zero_slot] = 0;   // list of step k-1, refilled by step k+1
@@ -504,7 +509,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
     const uint32_t my_cell = (uint32_t)tid / G, my_j = (uint32_t)tid % G;
     const bool leader = my_j == 0;
 
-    uint32_t next_raw = fetch_count(a, blockIdx.x, my_cell, leader);
+    uint32_t next_raw = fetch_count<SINGLE>(a, blockIdx.x, my_cell, leader);
     for (uint32_t tile = blockIdx.x; tile < a.num_tiles; tile += gridDim.x) {
         if (tid == 0) {
             int bi = 0;
@@ -557,7 +562,18 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                 L.ng[my_cell] = mine_g;
             }
         }
-        next_raw = fetch_count(a, tile + gridDim.x, my_cell, leader);
+        next_raw = fetch_count<SINGLE>(a, tile + gridDim.x, my_cell, leader);
+        // SRD rotation axes (and the wall side for the pressure estimator) of the
+        // tile's cells, one thread per cell; read after the scan's barriers
+        if (ALGO == 0) {
+            for (uint32_t i = (uint32_t)tid; i < nc; i += kThreads) {
+                const uint3 cc = storage_coords(b, c0 + i);
+                const float3 ax = D::srd_axis(a, b, step, ref_index(b, cc));
+                uint32_t side = 0;
+                if (a.pressure && b.wall_z) side = cc.z <= 1u ? 1u : (cc.z + 2u >= (uint32_t)b.L[2] ? 2u : 0u);
+                L.c1[i] = make_float4(ax.x, ax.y, ax.z, __uint_as_float(side));
+            }
+        }
         // one scan of (particles << 16 | ghosts): a tile holds fewer than 2^16 of either
         uint32_t packed_total;
         const uint32_t packed = block_exclusive_scan(((mine + mine_g) << 16) | mine_g, warp_tot, packed_total);
@@ -606,7 +622,8 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                     bulk_g2s(s_pos + o, a.in_pos + src, n * 16u, &bar);
                     bulk_g2s(s_vel + o, a.in_vel + src, n * 16u, &bar);
                 }
-                for (uint32_t p = o + my_j; p < e; p += G) s_cell[p] = (uint16_t)i;
+                for (uint32_t p = o + my_j; p < e; p += G)   // cell of the entry, kGhostFlag on ghosts
+                    s_cell[p] = (uint16_t)(i | (p - o >= n ? kGhostFlag : 0u));
             }
             // ghosts, one thread per ghost (overlaps the copies)
             {
@@ -648,10 +665,11 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
             // extended: rank of every real particle within its cell by particle id
             if (ALGO == 1) {
                 for (uint32_t p = tid; p < np; p += kThreads) {
-                    const uint32_t ci = s_cell[p];
+                    const uint32_t info = s_cell[p];
+                    const uint32_t ci = info & ~kGhostFlag;
                     const uint32_t o = L.off[ci] - pbase;
                     const uint32_t n = L.cnt[ci];
-                    if (p - o < n) {
+                    if (!(info & kGhostFlag)) {
                         const uint32_t id = __float_as_uint(s_vel[p].w);
                         uint32_t rank = 0;
                         for (uint32_t q = 0; q < n; ++q) rank += __float_as_uint(s_vel[o + q].w) < id;
@@ -678,15 +696,13 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                 sy = group_sum(sy, G);
                 sz = group_sum(sz, G);
                 if (in_sub && leader) {
-                    float3 mean = make_float3(0, 0, 0), axis = make_float3(0, 0, 0);
+                    float3 mean = make_float3(0, 0, 0);
                     if (n > 1) {
                         const float inv = 1.0f / (float)n;
                         mean = make_float3((__ll2float_rn(sx) * 0x1p-32f) * inv, (__ll2float_rn(sy) * 0x1p-32f) * inv,
                                            (__ll2float_rn(sz) * 0x1p-32f) * inv);
-                        axis = D::srd_axis(a, b, step, ref_index(b, storage_coords(b, c0 + i)));
                     }
-                    L.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));
-                    L.c1[i] = make_float4(axis.x, axis.y, axis.z, 0.0f);
+                    L.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));   // axis: c1, drawn per tile
                     if (!REPLAY && a.tape_ncell) a.tape_ncell[b.cell_base + c0 + i] = n > 1 ? n : 0u;
                 }
             } else if (in_sub && leader) {
@@ -697,17 +713,23 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                 const uint32_t n = min(cnt + g, b.cap);
                 const uint32_t m = n - g;   // real participants (lowest ids)
                 float3 com = make_float3(0, 0, 0), mean = make_float3(0, 0, 0), omega = make_float3(0, 0, 0);
+                uint32_t side = 0;   // wall layer of the cell for the pressure estimator: 1 bottom, 2 top
+                if (!REPLAY && a.pressure && b.wall_z)
+                    side = cc.z <= 1u ? 1u : (cc.z + 2u >= (uint32_t)b.L[2] ? 2u : 0u);
                 if (n > 1) {
                     const float3 centre = cell_centre(b, cc);
                     float gate;
                     const float3 axis = D::ext_axis(a, b, step, ref, gate);
                     auto at = [&](uint32_t k) -> uint32_t { return k < m ? s_inv[o + k] : o + cnt + (k - m); };
+                    float real_vz = 0.0f;
                     for (uint32_t k = 0; k < n; ++k) {
                         const uint32_t p = at(k);
                         const float4 xp = s_pos[p], vp = s_vel[p];
                         com.x += (xp.x - centre.x); com.y += (xp.y - centre.y); com.z += (xp.z - centre.z);
                         mean.x += vp.x; mean.y += vp.y; mean.z += vp.z;
+                        if (k < m) real_vz += vp.z;
                     }
+                    if (side) imp[side - 1] -= (side == 1 ? 1.0f : -1.0f) * real_vz;
                     const float inv = 1.0f / (float)n;
                     com = make_float3(com.x * inv + centre.x, com.y * inv + centre.y, com.z * inv + centre.z);
                     mean = make_float3(mean.x * inv, mean.y * inv, mean.z * inv);
@@ -779,7 +801,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                     }
                 }
                 L.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));
-                L.c1[i] = make_float4(com.x, com.y, com.z, 0.0f);
+                L.c1[i] = make_float4(com.x, com.y, com.z, __uint_as_float(side));
                 L.omega[i] = make_float4(omega.x, omega.y, omega.z, __uint_as_float(m));
             }
             __syncthreads();
@@ -790,8 +812,9 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                 bool active = false;
                 uint32_t ci = 0;
                 if (p < np) {
-                    ci = s_cell[p];
-                    active = p - (L.off[ci] - pbase) < L.cnt[ci];
+                    const uint32_t info = s_cell[p];
+                    ci = info & ~kGhostFlag;
+                    active = !(info & kGhostFlag);
                 }
                 float3 x = make_float3(0, 0, 0), v = make_float3(0, 0, 0);
                 if (active) {
@@ -836,6 +859,18 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                     } else {
                         float3 vn = v;
                         const float3 xn = stream_shift(b, x, vn, sn);
+                        if (a.pressure) {
+                            // collision in a wall-layer cell: the ghosts took up minus the
+                            // real particles' z momentum change (extended: the leader has
+                            // subtracted the participants' momentum before the collision)
+                            const uint32_t side = __float_as_uint(k1.w);
+                            if (side) {
+                                const float sg = side == 1 ? 1.0f : -1.0f;
+                                if (ALGO == 0) imp[side - 1] += sg * (v.z - vp.z);
+                                else if (n > 1 && s_rank[p] < __float_as_uint(L.omega[ci].w)) imp[side - 1] += sg * v.z;
+                            }
+                            if (b.wall_z && vn.z != v.z) imp[v.z > 0.0f ? 1 : 0] += 2.0f * fabsf(v.z);   // bounce-back
+                        }
                         s_key[p] = b.cell_base + storage_index(b, cell_of(b, xn));
                         s_pos[p] = make_float4(xn.x, xn.y, xn.z, 0.0f);
                         s_vel[p] = make_float4(vn.x, vn.y, vn.z, vp.w);
@@ -864,8 +899,13 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
             // result is used), then write the particles to their buckets
             {
                 uint32_t key[kMaxPerThread], peers[kMaxPerThread], base[kMaxPerThread];
+                const int jmax = (int)((np + kThreads - 1) / kThreads);   // the same for every thread
 #pragma unroll
                 for (int j = 0; j < kMaxPerThread; ++j) {
+                    key[j] = kNoKey;
+                    peers[j] = 0;
+                    base[j] = 0;
+                    if (j >= jmax) continue;
                     const uint32_t p = (uint32_t)tid + (uint32_t)kThreads * j;
                     key[j] = p < np ? s_key[p] : kNoKey;
                     const bool act = key[j] != kNoKey;
@@ -879,7 +919,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                 }
 #pragma unroll
                 for (int j = 0; j < kMaxPerThread; ++j) {
-                    if (key[j] == kNoKey) continue;
+                    if (j >= jmax || key[j] == kNoKey) continue;
                     const uint32_t p = (uint32_t)tid + (uint32_t)kThreads * j;
                     const uint32_t slot =
                         __shfl_sync(peers[j], base[j], __ffs(peers[j]) - 1) + __popc(peers[j] & lanemask_lt());
@@ -902,6 +942,14 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
             }
             __syncthreads();
             i0 = i1;
+        }
+    }
+    if (a.pressure) {
+#pragma unroll
+        for (int w = 0; w < 2; ++w) {
+            float v = imp[w];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+            if (lane == 0 && v != 0.0f) atomicAdd(&a.state->wall_impulse[w], (double)v);
         }
     }
 }
@@ -1298,18 +1346,33 @@ cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t p
 
 cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* blocks_per_sm)
 {
+    // The shared-memory limit is an attribute of the kernel function, shared by
+    // every handle of the process: it only ever grows, to the largest tile any
+    // handle uses (per device: the attribute is per context).
+    static std::mutex mu;
+    static size_t granted[64] = {};
     const size_t smem = step_smem_bytes(pbuf, cells, algorithm);
-    for (int i = 0; i < 2; ++i)
-        for (int j = 0; j < 2; ++j)
-            for (int k = 0; k < 2; ++k)
-                for (int r = 0; r < 2; ++r) {
-                    cudaError_t e = cudaFuncSetAttribute((const void*)kStepFns[i][j][k][r],
-                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                    if (e != cudaSuccess) return e;
-                }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        const int slot = dev & 63;
+        if (smem > granted[slot]) {
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j)
+                    for (int k = 0; k < 2; ++k)
+                        for (int r = 0; r < 2; ++r) {
+                            e = cudaFuncSetAttribute((const void*)kStepFns[i][j][k][r],
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                            if (e != cudaSuccess) return e;
+                        }
+            granted[slot] = smem;
+        }
+    }
     // load the kernels that step graphs capture before any capture begins
     cudaFuncAttributes attr;
-    cudaError_t e = cudaFuncGetAttributes(&attr, (const void*)advance_kernel);
+    e = cudaFuncGetAttributes(&attr, (const void*)advance_kernel);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, (const void*)sample_finalize_kernel);
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(

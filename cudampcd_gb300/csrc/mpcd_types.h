@@ -24,6 +24,7 @@ constexpr int kMaxInjectedShifts = 4;
 struct BoxDesc {
     int32_t L[3];          // container size incl. wall layers
     float Lf[3];
+    float L15[3], L2x[3], L3x[3], Lh[3];   // 1.5 L, 2 L, 3 L, L / 2 (float products, as the reference forms them)
     int32_t periodic[3];
     int32_t wall_z;        // periodicity.z == 0: bounce-back walls and ghost layers in z
     int32_t channel;       // ExperimentType::channel
@@ -61,6 +62,7 @@ struct DeviceState {
     float inject_shift[kMaxInjectedShifts][4];
     unsigned int inject_valid[kMaxInjectedShifts];
     unsigned long long step_base;        // graph replays: absolute step of the replay's first step
+    double wall_impulse[2];              // pressure estimator: outward impulse on the z walls {bottom, top}
 };
 
 enum : unsigned int {
@@ -125,6 +127,9 @@ struct StepArgs {
     uint32_t* tape_key;
     uint32_t* tape_lab;
     uint32_t* tape_ncell;
+    // pressure estimator on: accumulate the z impulse the fluid gives the walls
+    // (bounce-backs and collisions in the wall-layer cells) into state->wall_impulse
+    int32_t pressure;
 };
 
 constexpr uint32_t kTapeNone = 0xFFFFFFFFu;

@@ -178,6 +178,21 @@ int32_t mpcd_gb_autotune(mpcd_gb_handle *h, int32_t steps_per_candidate, uint32_
 int32_t mpcd_gb_set_particles_device(mpcd_gb_handle *h, const float *d_positions, const float *d_velocities);
 int32_t mpcd_gb_get_particles_device(mpcd_gb_handle *h, float *d_positions, float *d_velocities);
 
+/* Continue from the current particle state with the step counter -- the key of every
+ * Philox draw -- set to `step` (< 2^40).  Two runs that start from the same state at the
+ * same step draw the same random numbers (common random numbers). */
+int32_t mpcd_gb_set_step(mpcd_gb_handle *h, uint64_t step);
+
+/* Wall pressure estimator (the reference has none).  It measures the momentum per unit
+ * area and time that the fluid gives each z wall, along the wall's outward normal:
+ *   - 2|v_z| for every bounce-back;
+ *   - the z momentum that the wall's ghost particles take up in the collisions of the
+ *     wall-layer cells (minus the real particles' change).
+ * In equilibrium this is the fluid's pressure; for SRD, an ideal gas, it is n T.
+ * restart != 0 zeroes the sums and measures from the next step on.  Every call returns
+ * out = {bottom wall, top wall, steps measured}.  Single box with walls in z. */
+int32_t mpcd_gb_wall_pressure(mpcd_gb_handle *h, int32_t restart, double out[3]);
+
 /* Body force (SimulationParameters::drag) of every box from the next step on. */
 int32_t mpcd_gb_set_drag(mpcd_gb_handle *h, float drag);
 

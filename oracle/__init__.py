@@ -21,6 +21,7 @@ _ref = None
 
 u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
 f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 
 STANDARD, CHANNEL = 0, 1
@@ -122,6 +123,8 @@ def lib():
         L.orc_run_create.restype = C.c_void_p
         L.orc_run_steps.argtypes = [C.c_void_p, C.c_int32]
         L.orc_run_steps.restype = C.c_int
+        L.orc_run_pressure_steps.argtypes = [C.c_void_p, C.c_int32, f64p, C.c_void_p]
+        L.orc_run_pressure_steps.restype = C.c_int
         L.orc_run_particles.argtypes = [C.c_void_p]
         L.orc_run_particles.restype = C.c_size_t
         L.orc_run_destroy.argtypes = [C.c_void_p]
@@ -360,6 +363,13 @@ class Run:
 
     def steps(self, n: int) -> None:
         if lib().orc_run_steps(self._h, n):
+            raise RuntimeError("oracle step failed")
+
+    def pressure_steps(self, n: int, impulse: np.ndarray, layer_count: np.ndarray | None = None) -> None:
+        """n steps, adding the outward wall impulses {bottom, top} to `impulse` and the
+        particles per lab z layer to `layer_count` (float64 arrays)."""
+        if lib().orc_run_pressure_steps(self._h, n, impulse,
+                                        None if layer_count is None else layer_count.ctypes.data):
             raise RuntimeError("oracle step failed")
 
     def close(self) -> None:

@@ -950,6 +950,64 @@ int orc_run_steps(orc_run *r, int32_t n)
     return orc_reference_steps(&r->p, r->pos, r->vel, r->cell, r->N, &r->rng, n, r->counter, r->table, NULL);
 }
 
+/* Wall pressure estimator (test infrastructure; the reference has none): the
+ * outward z impulse the fluid gives the walls over n reference steps,
+ * impulse[0] bottom, impulse[1] top: 2|v_z| per bounce-back in translate
+ * (simulation_functions.cpp:53-82), and minus the real particles' z momentum
+ * change in the collisions of the two wall layers on each side, whose ghost
+ * particles stand for the wall (simulation_functions.cpp:116-167, 137-138).
+ * The collision cell is taken before the collision, which writes the particle's
+ * new cell back (simulation_functions.cpp:191-200, 395-400).
+ * layer_count (Lz entries, may be NULL) accumulates the particles per z layer
+ * of the lab grid after every step. */
+int orc_run_pressure_steps(orc_run *r, int32_t n, double impulse[2], double *layer_count)
+{
+    const orc_params *p = &r->p;
+    const size_t N = r->N;
+    const uint32_t Lxy = (uint32_t)(p->L[0] * p->L[1]);
+    const uint32_t Lz = (uint32_t)p->L[2];
+    float *vz = (float *)malloc(sizeof(float) * N);
+    uint32_t *cz = (uint32_t *)malloc(sizeof(uint32_t) * N);   /* collision cell z: the collision rewrites cell[] */
+    if (!vz || !cz) {
+        free(vz);
+        free(cz);
+        return -1;
+    }
+    orc_draws d;
+    memset(&d, 0, sizeof d);
+    d.mode = ORC_DRAWS_XOSHIRO;
+    d.rng = &r->rng;
+    int rc = 0;
+    for (int32_t s = 0; s < n && !rc; ++s) {
+        float shift[3];
+        shift[0] = orc_xoshiro_uniform(&r->rng) - 0.5f;
+        shift[1] = orc_xoshiro_uniform(&r->rng) - 0.5f;
+        shift[2] = orc_xoshiro_uniform(&r->rng) - 0.5f;
+        memset(r->counter, 0, sizeof(uint32_t) * r->C);
+        for (size_t i = 0; i < N; ++i) vz[i] = r->vel[3 * i + 2];
+        orc_translate(p, r->pos, r->vel, r->cell, N, shift, r->counter, r->table);
+        for (size_t i = 0; i < N; ++i)
+            if (!p->periodic[2] && r->vel[3 * i + 2] != vz[i]) impulse[vz[i] > 0 ? 1 : 0] += 2.0 * fabs((double)vz[i]);
+        for (size_t i = 0; i < N; ++i) {
+            vz[i] = r->vel[3 * i + 2];
+            cz[i] = r->cell[i] / Lxy;
+        }
+        rc = p->algorithm == ORC_SRD
+                 ? orc_srd_collision(p, r->pos, r->vel, r->cell, N, shift, r->counter, r->table, &d)
+                 : orc_extended_collision(p, r->pos, r->vel, r->cell, N, shift, r->counter, r->table, &d);
+        for (size_t i = 0; i < N && !p->periodic[2]; ++i) {
+            const double dv = (double)r->vel[3 * i + 2] - (double)vz[i];
+            if (cz[i] <= 1) impulse[0] += dv;
+            else if (cz[i] + 2 >= Lz) impulse[1] -= dv;
+        }
+        if (layer_count)
+            for (size_t i = 0; i < N; ++i) layer_count[orc_cell_index(p, r->pos + 3 * i) / Lxy] += 1.0;
+    }
+    free(vz);
+    free(cz);
+    return rc;
+}
+
 size_t orc_run_particles(const orc_run *r) { return r->N; }
 
 void orc_run_destroy(orc_run *r)

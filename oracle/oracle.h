@@ -160,6 +160,10 @@ typedef struct orc_run orc_run;
 orc_run *orc_run_create(const orc_params *p, uint64_t seed);
 int orc_run_steps(orc_run *r, int32_t n);
 size_t orc_run_particles(const orc_run *r);
+/* Wall pressure estimator over n steps: outward z impulse on {bottom, top} walls
+ * (bounce-backs + wall-layer collisions); layer_count[Lz] (or NULL) accumulates the
+ * particles per lab z layer after every step. */
+int orc_run_pressure_steps(orc_run *r, int32_t n, double impulse[2], double *layer_count);
 void orc_run_destroy(orc_run *r);
 
 #ifdef __cplusplus

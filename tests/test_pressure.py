@@ -1,0 +1,82 @@
+"""Wall pressure and density profile (equation of state) against theory and the reference.
+
+The reference has no pressure measurement.  The estimator (mpcd_gb_wall_pressure)
+is the momentum per unit area and time that the fluid gives the two z walls:
+bounce-backs plus the momentum the wall ghosts take up in collisions.  It is
+applied identically to the oracle's restatement of the reference CPU step
+(orc_run_pressure_steps, reference Xoshiro draws).
+- SRD is an ideal gas: its pressure must be n T.
+- The extended MPC collision (stochastic gate, non-ideal equation of state) must
+  give the reference's pressure and density profile within statistical error.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle as O
+from cudampcd_gb300 import capi
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_blocks(alg, L, n, steps, blocks, seed, T=1.0):
+    h = capi.Handle(L=L, periodic=(1, 1, 0), n=n, dt=0.02, drag=0.0, temperature=T, algorithm=alg, seed=seed)
+    try:
+        h.step(300)
+        P = []
+        for _ in range(blocks):
+            h.wall_pressure(restart=True)
+            h.step(steps)
+            p0, p1, k = h.wall_pressure()
+            assert k == steps
+            P.append((p0 + p1) / 2)
+        h.step_and_sample(steps * blocks)
+        density, _ = h.sample_mean()
+        S = steps * blocks
+        layers = density.reshape(L[2], L[1], L[0]).mean(axis=(1, 2)) * (S - 1) / S
+        assert h.counters()[1] == 0
+    finally:
+        h.close()
+    P = np.array(P)
+    return P.mean(), P.std(ddof=1) / np.sqrt(len(P)), layers
+
+
+def oracle_blocks(alg, L, n, steps, blocks, seed):
+    box = O.Box(L=L, periodic=(1, 1, 0), n=n, dt=0.02, drag=0.0, algorithm=alg)
+    r = O.Run(box, seed)
+    try:
+        imp = np.zeros(2)
+        r.pressure_steps(300, imp)
+        P, layers = [], np.zeros(L[2])
+        for _ in range(blocks):
+            imp[:] = 0.0
+            r.pressure_steps(steps, imp, layers)
+            P.append(imp.mean() / (L[0] * L[1] * steps * 0.02))
+    finally:
+        r.close()
+    P = np.array(P)
+    return P.mean(), P.std(ddof=1) / np.sqrt(len(P)), layers / (L[0] * L[1] * steps * blocks)
+
+
+def test_srd_wall_pressure_is_the_ideal_gas_pressure():
+    n, T = 10, 1.3
+    P, err, layers = gpu_blocks(0, (16, 16, 22), n, 2000, 10, seed=4, T=T)
+    print(f"SRD wall pressure {P:.4f} +- {err:.4f}, n T = {n * T}")
+    assert abs(P - n * T) < max(4 * err, 1e-3 * n * T)
+    assert abs(P / (n * T) - 1) < 0.01
+    fluid = layers[1:-1]
+    # the wall layers stay (nearly) empty: only lone particles, which keep their shifted
+    # position (simulation_functions.cpp:169-191), are sampled there
+    assert np.all(np.abs(fluid / n - 1) < 0.03) and layers[0] < 1e-3 and layers[-1] < 1e-3
+
+
+def test_extended_pressure_and_density_match_the_reference_cpu_step():
+    L, n = (8, 8, 12), 10
+    Pg, eg, lg = gpu_blocks(1, L, n, 4000, 16, seed=6)
+    Po, eo, lo = oracle_blocks(O.EXTENDED, L, n, 1000, 8, seed=6)
+    sigma = np.hypot(eg, eo)
+    print(f"extended MPC wall pressure: GPU {Pg:.4f} +- {eg:.4f}, reference CPU step {Po:.4f} +- {eo:.4f}, "
+          f"n T = {n}; density layers GPU {np.round(lg[1:-1], 3)} reference {np.round(lo[1:-1], 3)}")
+    assert abs(Pg - Po) < 4 * sigma
+    assert np.all(np.abs(lg[1:-1] - lo[1:-1]) < 0.05 * n)
