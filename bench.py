@@ -309,16 +309,17 @@ def run_gpu_arm(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
-def ensemble_boxes(R: int, seed: int = 0):
-    """The replicas of the batched workload (numpy default_rng(seed))."""
+def ensemble_boxes(R: int, seed: int = 0, small: bool = False):
+    """The replicas of the batched workload (numpy default_rng(seed)); `small`:
+    Lx, Ly in {8, 16}, Lz in [20, 60], n in {5, 10} instead."""
     import numpy as np
 
     rng = np.random.default_rng(seed)
     boxes = []
     for r in range(R):
-        lx, ly = (int(v) for v in rng.choice([8, 16, 32, 64], size=2))
-        lz = int(rng.integers(20, 201))
-        n = int(rng.choice([5, 10, 20]))
+        lx, ly = (int(v) for v in rng.choice([8, 16] if small else [8, 16, 32, 64], size=2))
+        lz = int(rng.integers(20, 61 if small else 201))
+        n = int(rng.choice([5, 10] if small else [5, 10, 20]))
         drag = float(10 ** rng.uniform(-4, -2))
         boxes.append(dict(L=(lx, ly, lz), periodic=(1, 1, 0), n=n, dt=0.02, drag=drag, temperature=1.0,
                           seed=1000 + r))
@@ -330,7 +331,7 @@ def run_ensemble(args):
 
     from cudampcd_gb300 import capi
 
-    boxes = ensemble_boxes(args.ensemble)
+    boxes = ensemble_boxes(args.ensemble, small=args.small_replicas)
     K = args.steps
     h = capi.Handle(boxes=boxes)
     N = h.N
@@ -359,9 +360,10 @@ def run_ensemble(args):
     out = {"metric": METRIC, "value": batched, "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": args.warmup,
            "ms_per_step": 1e3 * t_batched / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32", "data": "synthetic",
-           "config": {"workload": f"batched SRD ensemble: {len(boxes)} channel replicas, N = {N}, "
-                                  "Lx,Ly in {8,16,32,64}, Lz in [20,200], n in {5,10,20}, drag log-uniform "
-                                  "[1e-4,1e-2], T=1, dt=0.02, seeds 1000+r (numpy default_rng(0))",
+           "config": {"workload": f"batched SRD ensemble: {len(boxes)} channel replicas, N = {N}, " +
+                                  ("Lx,Ly in {8,16}, Lz in [20,60], n in {5,10}" if args.small_replicas else
+                                   "Lx,Ly in {8,16,32,64}, Lz in [20,200], n in {5,10,20}") +
+                                  ", drag log-uniform [1e-4,1e-2], T=1, dt=0.02, seeds 1000+r (numpy default_rng(0))",
                       "tiles": {"cells_per_tile": tile_cells, "particle_buffer": pbuf},
                       "timing": "host wall clock around step(K) + synchronize, both arms"},
            "batched_vs_sequential": {"batched": batched, "sequential": sequential, "speedup": batched / sequential},
@@ -426,6 +428,7 @@ def main():
     ap.add_argument("--size", type=int, nargs=3, metavar=("LX", "LY", "LZ"))
     ap.add_argument("--algorithm", default="srd", choices=["srd", "extended"])
     ap.add_argument("--ensemble", type=int, default=0, metavar="R")
+    ap.add_argument("--small-replicas", dest="small_replicas", action="store_true")
     ap.add_argument("--physics", choices=["extended", "srd"])
     args = ap.parse_args()
     if args.warmup < 3:

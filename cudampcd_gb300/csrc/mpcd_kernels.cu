@@ -351,14 +351,14 @@ constexpr uint32_t kGhostFlag = 0x8000u;   // s_cell entries of ghost particles 
 constexpr int kMaxPerThread = 8;   // particle buffer <= kMaxPerThread * kThreads
 
 // Shared memory of one CTA, carved from the dynamic allocation:
-//   particles: pos, vel (float4), next key (u32), cell (u16)
+//   particles: pos (float4; after the collision pass .w holds the next cell key),
+//              vel (float4), cell (u16)
 //   extended only: rank (u16), stable index (u16)
 //   cells: cnt, ng, off, goff (u32, T + 1 each), c0, c1 (float4, T each)
 //   extended only: omega (float4, T)
 struct TileLayout {
     float4* pos;
     float4* vel;
-    uint32_t* key;
     uint16_t* cell;
     uint16_t* rank;
     uint16_t* inv;
@@ -368,7 +368,7 @@ struct TileLayout {
 
 __host__ __device__ inline size_t tile_smem_bytes(uint32_t pbuf, uint32_t cells, int algorithm)
 {
-    const size_t per_particle = 16 + 16 + 4 + 2 + (algorithm ? 4 : 0);
+    const size_t per_particle = 16 + 16 + 2 + (algorithm ? 4 : 0);
     size_t bytes = (size_t)pbuf * per_particle;
     bytes = (bytes + 15) / 16 * 16 + 4 * (size_t)(cells + 1) * 4;
     bytes = (bytes + 15) / 16 * 16 + (size_t)cells * 16 * (algorithm ? 3 : 2);
@@ -380,11 +380,10 @@ __device__ inline TileLayout carve(unsigned char* base, uint32_t pbuf, uint32_t 
     TileLayout t;
     t.pos = reinterpret_cast<float4*>(base);
     t.vel = t.pos + pbuf;
-    t.key = reinterpret_cast<uint32_t*>(t.vel + pbuf);
-    t.cell = reinterpret_cast<uint16_t*>(t.key + pbuf);
+    t.cell = reinterpret_cast<uint16_t*>(t.vel + pbuf);
     t.rank = t.cell + pbuf;
     t.inv = t.rank + (algorithm ? pbuf : 0);
-    size_t at = (size_t)pbuf * (16 + 16 + 4 + 2 + (algorithm ? 4 : 0));
+    size_t at = (size_t)pbuf * (16 + 16 + 2 + (algorithm ? 4 : 0));
     at = (at + 15) / 16 * 16;
     uint32_t* u = reinterpret_cast<uint32_t*>(base + at);
     t.cnt = u;
@@ -398,18 +397,28 @@ __device__ inline TileLayout carve(unsigned char* base, uint32_t pbuf, uint32_t 
     return t;
 }
 
-// Count of cell `c` of `tile` (first thread of the cell's group); issued one
-// tile ahead so its latency hides.  Outside a replay it also clears the same
-// cell of the counts of step k-1, which step k+1 will fill.
+// First global cell and cell count of `tile`, and its box (one thread per CTA).
 template <bool SINGLE>
-__device__ __forceinline__ uint32_t fetch_count(const StepArgs& a, uint32_t tile, uint32_t c, bool leader)
+__device__ __forceinline__ void locate_tile(const StepArgs& a, uint32_t tile, uint32_t& first, uint32_t& nc, int& bi)
 {
-    if (!leader || tile >= a.num_tiles) return 0;
-    int bi = 0;
+    bi = 0;
+    first = 0;
+    nc = 0;
+    if (tile >= a.num_tiles) return;
     const BoxDesc* bp = SINGLE ? &a.box0 : find_box(a, tile, bi);
     const uint32_t c0 = (tile - bp->tile_base) * bp->tile_cells;
-    if (c >= min(bp->tile_cells, bp->C - c0)) return 0;
-    const uint32_t g = bp->cell_base + c0 + c;
+    first = bp->cell_base + c0;
+    nc = min(bp->tile_cells, bp->C - c0);
+}
+
+// Count of cell `c` of a tile (first thread of the cell's group); issued one
+// tile ahead so its latency hides.  Outside a replay it also clears the same
+// cell of the counts of step k-1, which step k+1 will fill.
+__device__ __forceinline__ uint32_t fetch_count(const StepArgs& a, uint32_t first, uint32_t nc, uint32_t c,
+                                                bool leader)
+{
+    if (!leader || c >= nc) return 0;
+    const uint32_t g = first + c;
     if (!a.replay) a.zero_count[g] = 0;
     return a.in_count[g];
 }
@@ -469,8 +478,10 @@ __device__ __forceinline__ T group_sum(T v, uint32_t G)
     return v;
 }
 
+// SRD: 4 CTAs of 256 threads per SM (64 registers, about 54 KB of shared memory each);
+// extended: 3 (its tile carries two more arrays)
 template <int ALGO, bool TABLE, bool SINGLE, bool REPLAY>
-__global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32_t pbuf)
+__global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const StepArgs a, uint32_t pbuf)
 {
     using D = Draws<TABLE>;
     extern __shared__ __align__(128) unsigned char dyn[];
@@ -483,7 +494,6 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
     const TileLayout L = carve(dyn, pbuf, tcells, ALGO);
     float4* const s_pos = L.pos;
     float4* const s_vel = L.vel;
-    uint32_t* const s_key = L.key;
     uint16_t* const s_cell = L.cell;
     uint16_t* const s_rank = L.rank;   // extended only
     uint16_t* const s_inv = L.inv;     // extended only
@@ -509,11 +519,16 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
     const uint32_t my_cell = (uint32_t)tid / G, my_j = (uint32_t)tid % G;
     const bool leader = my_j == 0;
 
-    uint32_t next_raw = fetch_count<SINGLE>(a, blockIdx.x, my_cell, leader);
+    // the tile after the current one: located by one thread, read by the cell leaders
+    __shared__ uint32_t s_next_first, s_next_nc;
+    __shared__ int s_next_box;
+    if (tid == 0) locate_tile<SINGLE>(a, blockIdx.x, s_next_first, s_next_nc, s_next_box);
+    __syncthreads();
+    uint32_t next_raw = fetch_count(a, s_next_first, s_next_nc, my_cell, leader);
     for (uint32_t tile = blockIdx.x; tile < a.num_tiles; tile += gridDim.x) {
         if (tid == 0) {
-            int bi = 0;
-            const BoxDesc* bp = SINGLE ? &a.box0 : find_box(a, tile, bi);
+            const int bi = s_next_box;   // located while the previous tile was processed
+            const BoxDesc* bp = SINGLE ? &a.box0 : &a.boxes[bi];
             if (bi != sbox_index) {   // box and its grid shifts change only between boxes
                 if (!SINGLE) sbox = *bp;
                 sbox_index = bi;
@@ -562,7 +577,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                 L.ng[my_cell] = mine_g;
             }
         }
-        next_raw = fetch_count<SINGLE>(a, tile + gridDim.x, my_cell, leader);
+        if (tid == 0) locate_tile<SINGLE>(a, tile + gridDim.x, s_next_first, s_next_nc, s_next_box);
         // SRD rotation axes (and the wall side for the pressure estimator) of the
         // tile's cells, one thread per cell; read after the scan's barriers
         if (ALGO == 0) {
@@ -577,6 +592,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
         // one scan of (particles << 16 | ghosts): a tile holds fewer than 2^16 of either
         uint32_t packed_total;
         const uint32_t packed = block_exclusive_scan(((mine + mine_g) << 16) | mine_g, warp_tot, packed_total);
+        next_raw = fetch_count(a, s_next_first, s_next_nc, my_cell, leader);   // after the scan's barriers
         if (leader && my_cell < nc) {
             L.off[my_cell] = packed >> 16;
             L.goff[my_cell] = packed & 0xFFFFu;
@@ -871,8 +887,8 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                             }
                             if (b.wall_z && vn.z != v.z) imp[v.z > 0.0f ? 1 : 0] += 2.0f * fabsf(v.z);   // bounce-back
                         }
-                        s_key[p] = b.cell_base + storage_index(b, cell_of(b, xn));
-                        s_pos[p] = make_float4(xn.x, xn.y, xn.z, 0.0f);
+                        const uint32_t next = b.cell_base + storage_index(b, cell_of(b, xn));
+                        s_pos[p] = make_float4(xn.x, xn.y, xn.z, __uint_as_float(next));
                         s_vel[p] = make_float4(vn.x, vn.y, vn.z, vp.w);
                         if (ALGO == 0 && a.tape_key) {
                             const uint32_t id = __float_as_uint(vp.w);
@@ -882,7 +898,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                         }
                     }
                 } else if (p < np) {
-                    s_key[p] = kNoKey;
+                    reinterpret_cast<uint32_t*>(s_pos + p)[3] = kNoKey;
                 }
                 if (!REPLAY && a.sample) {
                     const uint32_t lab = active ? b.cell_base + ref_index(b, cell_of(b, x)) : 0;
@@ -907,7 +923,7 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                     base[j] = 0;
                     if (j >= jmax) continue;
                     const uint32_t p = (uint32_t)tid + (uint32_t)kThreads * j;
-                    key[j] = p < np ? s_key[p] : kNoKey;
+                    key[j] = p < np ? __float_as_uint(s_pos[p].w) : kNoKey;
                     const bool act = key[j] != kNoKey;
                     const unsigned m = __ballot_sync(kFull, act);
                     peers[j] = 0;
@@ -923,7 +939,8 @@ __global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a, uint32
                     const uint32_t p = (uint32_t)tid + (uint32_t)kThreads * j;
                     const uint32_t slot =
                         __shfl_sync(peers[j], base[j], __ffs(peers[j]) - 1) + __popc(peers[j] & lanemask_lt());
-                    const float4 xp = s_pos[p], vp = s_vel[p];
+                    const float4 xs = s_pos[p], vp = s_vel[p];
+                    const float4 xp = make_float4(xs.x, xs.y, xs.z, 0.0f);
                     if (slot < b.cap) {
                         const uint64_t at = b.slot_base + (uint64_t)(key[j] - b.cell_base) * b.cap + slot;
                         a.out_pos[at] = xp;
@@ -1365,6 +1382,9 @@ cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* bl
                         for (int r = 0; r < 2; ++r) {
                             e = cudaFuncSetAttribute((const void*)kStepFns[i][j][k][r],
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                            if (e == cudaSuccess)   // all of the unified L1/shared array as shared memory
+                                e = cudaFuncSetAttribute((const void*)kStepFns[i][j][k][r],
+                                                         cudaFuncAttributePreferredSharedMemoryCarveout, 100);
                             if (e != cudaSuccess) return e;
                         }
             granted[slot] = smem;
