@@ -19,7 +19,9 @@ Physics: --physics extended runs the extended-MPC channel with the non-ideal
 equation of state (256 x 256 x 64 cells + 2 walls, n = 20, T = 1, dt = 0.02,
 g = 0.0005): warm-up, then the wall pressure, the density profile and the
 viscosity from the curvature of the sampled velocity profile.  --physics srd
-runs the same measurement with the SRD collision.
+runs the same measurement with the SRD collision.  --eta-guess E starts the
+flow from the steady Poiseuille profile of viscosity E (the warm-up then only
+has to relax the guess's error).
 
 Profiling options (the default run uses none of them): --size LX LY LZ replaces
 the fluid cells of the workload (walls are added in z), --algorithm extended
@@ -380,6 +382,13 @@ def run_physics(args):
     Lx, Ly, Lz = (args.size or (256, 256, 64))
     n, g, dt = 20, 0.0005, 0.02
     h = capi.Handle(L=(Lx, Ly, Lz + 2), periodic=(1, 1, 0), n=n, dt=dt, drag=g, algorithm=alg, seed=0)
+    if args.eta_guess:   # start from the steady profile of a guessed viscosity: a shorter warm-up
+        vel = h.velocities()
+        z = h.positions()[:, 2].astype(np.float64)
+        hz = Lz / 2.0
+        vel[:, 0] += (n * g * (hz * hz - z * z) / (2.0 * args.eta_guess)).astype(np.float32)
+        h.set_velocities(vel)
+        del vel, z
     t0 = time.perf_counter()
     h.step(args.warmup)
     h.synchronize()
@@ -405,6 +414,7 @@ def run_physics(args):
     out = {"physics": args.physics, "workload": f"{args.physics} channel {Lx}x{Ly}x{Lz} cells + 2 walls, n={n}, "
                                                 f"T=1, dt={dt}, g={g}, N={h.N}",
            "warmup_steps": args.warmup, "sampled_steps": blocks * per, "warmup_s": t_warm,
+           "initial_profile_eta": args.eta_guess,
            "wall_pressure": {"mean": float(P.mean()), "stderr": float(P.std(ddof=1) / np.sqrt(blocks)),
                              "ideal_gas_nT": float(n)},
            "viscosity": {"mean": float(etas.mean()), "stderr": float(etas.std(ddof=1) / np.sqrt(blocks)),
@@ -430,6 +440,7 @@ def main():
     ap.add_argument("--ensemble", type=int, default=0, metavar="R")
     ap.add_argument("--small-replicas", dest="small_replicas", action="store_true")
     ap.add_argument("--physics", choices=["extended", "srd"])
+    ap.add_argument("--eta-guess", dest="eta_guess", type=float, default=0.0)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")

@@ -78,6 +78,8 @@ def lib() -> C.CDLL:
         L.mpcd_gb_get_particles_device.argtypes = [H, C.c_void_p, C.c_void_p]
         L.mpcd_gb_set_drag.argtypes = [H, C.c_float]
         L.mpcd_gb_set_step.argtypes = [H, C.c_uint64]
+        L.mpcd_gb_save_snapshot.argtypes = [H, C.c_char_p]
+        L.mpcd_gb_load_snapshot.argtypes = [H, C.c_char_p]
         L.mpcd_gb_wall_pressure.argtypes = [H, C.c_int32, np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")]
         L.mpcd_gb_profile_forward.argtypes = [H, C.c_int32, C.c_int32, C.c_void_p]
         L.mpcd_gb_profile_backward.argtypes = [H, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
@@ -237,6 +239,12 @@ class Handle:
     def get_particles_device(self, d_pos, d_vel):
         self._check(self._lib.mpcd_gb_get_particles_device(self.h, C.c_void_p(d_pos or None),
                                                            C.c_void_p(d_vel or None)))
+
+    def save_snapshot(self, path):
+        self._check(self._lib.mpcd_gb_save_snapshot(self.h, str(path).encode()))
+
+    def load_snapshot(self, path):
+        self._check(self._lib.mpcd_gb_load_snapshot(self.h, str(path).encode()))
 
     def set_step(self, step):
         self._check(self._lib.mpcd_gb_set_step(self.h, int(step)))

@@ -81,8 +81,20 @@ __device__ __forceinline__ float pbc1(float r, float L, float L15, float L2, flo
     return m - Lh;
 }
 
+// Fast path of pbc1 without its range check.
+__device__ __forceinline__ float pbc1_fast(float a, float L, float L2)
+{
+    return a - (a >= L2 ? L2 : (a >= L ? L : 0.0f));
+}
+
+// All three axes; one branch to the fmodf path when any a = r + 1.5L leaves [0, 3L).
 __device__ __forceinline__ float3 pbc(const BoxDesc& b, float3 r)
 {
+    const float ax = r.x + b.L15[0], ay = r.y + b.L15[1], az = r.z + b.L15[2];
+    const bool in = (ax >= 0.0f) & (ax < b.L3x[0]) & (ay >= 0.0f) & (ay < b.L3x[1]) & (az >= 0.0f) & (az < b.L3x[2]);
+    if (__builtin_expect(in, 1))
+        return make_float3(pbc1_fast(ax, b.Lf[0], b.L2x[0]) - b.Lh[0], pbc1_fast(ay, b.Lf[1], b.L2x[1]) - b.Lh[1],
+                           pbc1_fast(az, b.Lf[2], b.L2x[2]) - b.Lh[2]);
     return make_float3(pbc1(r.x, b.Lf[0], b.L15[0], b.L2x[0], b.L3x[0], b.Lh[0]),
                        pbc1(r.y, b.Lf[1], b.L15[1], b.L2x[1], b.L3x[1], b.Lh[1]),
                        pbc1(r.z, b.Lf[2], b.L15[2], b.L2x[2], b.L3x[2], b.Lh[2]));
@@ -97,6 +109,24 @@ __device__ __forceinline__ uint32_t cell_coord(float x, float Lf, float Lh, uint
     c = c == L ? 0u : c;
     if (__builtin_expect(!(f >= 0.0f && f <= Lf), 0)) c = (uint32_t)(long long)f % L;
     return c;
+}
+
+// Cell of a position that pbc() produced: x + L/2 lies in [0, L] unless pbc()
+// took its fmodf path on a wildly out-of-box argument; one unsigned compare
+// routes that case to the general conversion.
+__device__ __forceinline__ uint32_t cell_coord_wrapped(float x, float Lh, uint32_t L)
+{
+    const float f = floorf(x + Lh);
+    const uint32_t c = (uint32_t)(int)f;
+    if (__builtin_expect(c < L, 1)) return c;
+    return c == L ? 0u : (uint32_t)(long long)f % L;
+}
+
+__device__ __forceinline__ uint3 cell_of_wrapped(const BoxDesc& b, float3 x)
+{
+    return make_uint3(cell_coord_wrapped(x.x, b.Lh[0], (uint32_t)b.L[0]),
+                      cell_coord_wrapped(x.y, b.Lh[1], (uint32_t)b.L[1]),
+                      cell_coord_wrapped(x.z, b.Lh[2], (uint32_t)b.L[2]));
 }
 
 __device__ __forceinline__ uint3 cell_of(const BoxDesc& b, float3 x)

@@ -294,6 +294,127 @@ public:
         out[2] = steps;
     }
 
+    // ------------------------------------------------------------ snapshots
+    //
+    // File layout (little-endian): "MPCDGBS1", u32 version = 1, u32 boxes, u64 step,
+    // u64 N, per box {i32 experiment, i32 algorithm, i32 periodicity[3], f32
+    // volume_size[3], u32 n, f32 delta_t, f32 temperature, f32 thermal_velocity,
+    // f32 drag, u64 seed}, f32 positions[3N], f32 velocities[3N] (post-step state by
+    // particle id), u64 FNV-1a of all preceding bytes.
+    struct SnapshotBox {
+        int32_t experiment, algorithm, periodicity[3];
+        float volume_size[3];
+        uint32_t n;
+        float delta_t, temperature, thermal_velocity, drag;
+        uint64_t seed;
+    };
+
+    static uint64_t fnv1a(uint64_t h, const void* data, size_t bytes)
+    {
+        const unsigned char* c = static_cast<const unsigned char*>(data);
+        for (size_t i = 0; i < bytes; ++i) h = (h ^ c[i]) * 0x100000001B3ull;
+        return h;
+    }
+
+    void save_snapshot(const char* path)
+    {
+        if (!path) throw Error(MPCD_GB_EINVAL, "null path");
+        std::vector<float> pos(3 * N_), vel(3 * N_);
+        get(pos.data(), vel.data());
+        std::FILE* f = std::fopen(path, "wb");
+        if (!f) throw Error(MPCD_GB_EINVAL, std::string("cannot open ") + path + " for writing");
+        uint64_t h = 0xCBF29CE484222325ull;
+        bool ok = true;
+        auto put = [&](const void* d, size_t bytes) {
+            h = fnv1a(h, d, bytes);
+            ok = ok && std::fwrite(d, 1, bytes, f) == bytes;
+        };
+        const uint32_t version = 1, boxes = (uint32_t)box_params_.size();
+        const uint64_t step = step_, n = N_;
+        put("MPCDGBS1", 8);
+        put(&version, 4);
+        put(&boxes, 4);
+        put(&step, 8);
+        put(&n, 8);
+        for (const mpcd_gb_params& p : box_params_) {
+            SnapshotBox b{};
+            b.experiment = p.experiment;
+            b.algorithm = p.algorithm;
+            for (int d = 0; d < 3; ++d) {
+                b.periodicity[d] = p.periodicity[d];
+                b.volume_size[d] = p.volume_size[d];
+            }
+            b.n = p.n;
+            b.delta_t = p.delta_t;
+            b.temperature = p.temperature;
+            b.thermal_velocity = p.thermal_velocity;
+            b.drag = p.drag;
+            b.seed = p.seed;
+            put(&b, sizeof b);
+        }
+        put(pos.data(), sizeof(float) * pos.size());
+        put(vel.data(), sizeof(float) * vel.size());
+        ok = ok && std::fwrite(&h, 1, 8, f) == 8;
+        ok = (std::fclose(f) == 0) && ok;
+        if (!ok) throw Error(MPCD_GB_EINVAL, std::string("write to ") + path + " failed");
+    }
+
+    void load_snapshot(const char* path)
+    {
+        if (!path) throw Error(MPCD_GB_EINVAL, "null path");
+        std::FILE* f = std::fopen(path, "rb");
+        if (!f) throw Error(MPCD_GB_EINVAL, std::string("cannot open ") + path);
+        uint64_t h = 0xCBF29CE484222325ull;
+        bool ok = true;
+        auto get_bytes = [&](void* d, size_t bytes) {
+            ok = ok && std::fread(d, 1, bytes, f) == bytes;
+            if (ok) h = fnv1a(h, d, bytes);
+        };
+        char magic[8] = {};
+        uint32_t version = 0, boxes = 0;
+        uint64_t step = 0, n = 0, stored = 0;
+        get_bytes(magic, 8);
+        get_bytes(&version, 4);
+        get_bytes(&boxes, 4);
+        get_bytes(&step, 8);
+        get_bytes(&n, 8);
+        auto fail = [&](const char* why) {
+            std::fclose(f);
+            throw Error(MPCD_GB_EINVAL, std::string("snapshot ") + path + ": " + why);
+        };
+        if (!ok || std::memcmp(magic, "MPCDGBS1", 8) != 0 || version != 1) fail("not a version-1 snapshot");
+        if (boxes != box_params_.size() || n != N_) fail("box count or particle count differs from the handle");
+        for (const mpcd_gb_params& p : box_params_) {
+            SnapshotBox b{};
+            get_bytes(&b, sizeof b);
+            bool same = ok && b.experiment == p.experiment && b.algorithm == p.algorithm && b.n == p.n &&
+                        b.delta_t == p.delta_t && b.thermal_velocity == p.thermal_velocity && b.drag == p.drag &&
+                        b.seed == p.seed;
+            for (int d = 0; d < 3; ++d)
+                same = same && b.periodicity[d] == p.periodicity[d] && b.volume_size[d] == p.volume_size[d];
+            if (!same) fail("box parameters or seed differ from the handle's");
+        }
+        std::vector<float> pos(3 * N_), vel(3 * N_);
+        get_bytes(pos.data(), sizeof(float) * pos.size());
+        get_bytes(vel.data(), sizeof(float) * vel.size());
+        const uint64_t computed = h;
+        ok = ok && std::fread(&stored, 1, 8, f) == 8;
+        if (!ok) fail("truncated");
+        if (stored != computed) fail("checksum mismatch");
+        std::fclose(f);
+        if (step >= (1ull << 40)) throw Error(MPCD_GB_EINVAL, "snapshot step index beyond 2^40");
+        step_ = step;
+        check(cudaMemcpyAsync(dense_pos_.p, pos.data(), sizeof(float) * 3 * N_, cudaMemcpyHostToDevice, stream_),
+              "snapshot positions");
+        check(cudaMemcpyAsync(dense_vel_.p, vel.data(), sizeof(float) * 3 * N_, cudaMemcpyHostToDevice, stream_),
+              "snapshot velocities");
+        scatter_dense();
+        check(cudaStreamSynchronize(stream_), "snapshot");
+        check_device_errors();
+        sampling_ = false;
+        adj_valid_ = false;
+    }
+
     // Body force of every box from the next step on.
     void set_drag(float drag)
     {
@@ -580,7 +701,7 @@ public:
         uint32_t best_tc = boxes_[0].tile_cells, best_pbuf = pbuf_;
         for (uint32_t pbuf : {1024u, 1536u, 2048u}) {
             if (pbuf < 5 * n_max) continue;
-            for (uint32_t tc = 8; tc <= 128; tc <<= 1) {
+            for (uint32_t tc = 8; tc <= (params_.algorithm == 1 ? 64u : 128u); tc <<= 1) {
                 if (tc * n_max > pbuf) continue;
                 retile(tc, pbuf);
                 launch_one_step(false);   // first launch of a configuration: not timed
@@ -703,7 +824,9 @@ private:
         // ghosts (cap + n = 5n) at least
         uint32_t pbuf = std::max(1536u, 5 * n_max);
         if (pbuf > 2048) throw Error(MPCD_GB_EINVAL, "n above 409: one cell and its ghosts must fit a tile");
-        uint32_t tc = 128;
+        // extended: at least 4 threads per cell (its fixed 4-lane reductions)
+        const uint32_t tc_max = params_.algorithm == 1 ? 64u : 128u;
+        uint32_t tc = tc_max;
         while (tc > 8 && tc * n_max * 1.15 > pbuf) tc >>= 1;
         // tuning overrides (used by the tuning sweeps)
         if (const char* e = std::getenv("MPCD_GB_PBUF")) {
@@ -712,7 +835,7 @@ private:
         }
         if (const char* e = std::getenv("MPCD_GB_TILE_CELLS")) {
             const uint32_t v = (uint32_t)std::strtoul(e, nullptr, 10);
-            if (v >= 1 && v <= 256 && (v & (v - 1)) == 0) tc = v;
+            if (v >= 8 && v <= tc_max && (v & (v - 1)) == 0) tc = v;
         }
         set_tiles(tc, pbuf);
         float table[13][3];
@@ -1310,6 +1433,16 @@ int32_t mpcd_gb_wall_pressure(mpcd_gb_handle* h, int32_t restart, double out[3])
 {
     if (!out) return MPCD_GB_EINVAL;
     return guarded(h, [&](mpcd_gb::Engine& e) { e.wall_pressure(restart != 0, out); });
+}
+
+int32_t mpcd_gb_save_snapshot(mpcd_gb_handle* h, const char* path)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.save_snapshot(path); });
+}
+
+int32_t mpcd_gb_load_snapshot(mpcd_gb_handle* h, const char* path)
+{
+    return guarded(h, [&](mpcd_gb::Engine& e) { e.load_snapshot(path); });
 }
 
 int32_t mpcd_gb_set_drag(mpcd_gb_handle* h, float drag)

@@ -450,25 +450,27 @@ __device__ void overflow_pass(const StepArgs& a, uint64_t step)
             } else {
                 vs = v;
                 xs = stream_shift(b, x, vs, grid_shift(b, bi, step + 1, a.state));
-                key = b.cell_base + storage_index(b, cell_of(b, xs));
+                key = b.cell_base + storage_index(b, cell_of_wrapped(b, xs));
                 if (a.pressure && b.wall_z && vs.z != v.z)   // bounce-back: 2 |v_z| outward
                     atomicAdd(&a.state->wall_impulse[v.z > 0.0f ? 1 : 0], 2.0 * fabs((double)v.z));
                 if (a.tape_key) {
                     const bool bounced = vs.x != v.x || vs.y != v.y || vs.z != v.z;
                     a.tape_key[id] = kTapeNone;
-                    a.tape_lab[id] = (b.cell_base + ref_index(b, cell_of(b, x))) | (bounced ? kTapeBounce : 0u);
+                    a.tape_lab[id] = (b.cell_base + ref_index(b, cell_of_wrapped(b, x))) | (bounced ? kTapeBounce : 0u);
                 }
             }
         }
         if (a.replay) continue;
         const BoxDesc& b = a.boxes[bi];
         if (a.sample) {
-            const uint32_t lab = active ? b.cell_base + ref_index(b, cell_of(b, x)) : 0;
+            const uint32_t lab = active ? b.cell_base + ref_index(b, cell_of_wrapped(b, x)) : 0;
             sample_add(a.samp, lab, v, active);
         }
         store_particle(a, b, xs, vs, id, key, active);
     }
 }
+
+constexpr int kExtLanes = 4;   // lanes per cell of the extended collision (tiles of <= 64 cells)
 
 // Sum over the G lanes of a cell group (G a power of two dividing 32).
 template <class T>
@@ -696,12 +698,90 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
                 __syncthreads();
             }
 
-            // per-cell collision quantities, one group per cell
+            // Per particle: finish the collision (SRD rotation or extended update), unshift,
+            // drag, lab-grid sample, stream step k+1 and find the next cell.  k0 = (mean,
+            // n), k1 = (axis or centre of mass, wall side) of the particle's cell ci.
+            auto finish = [&](uint32_t p, uint32_t ci, const float4 k0, const float4 k1) {
+                const float4 xp = s_pos[p], vp = s_vel[p];
+                float3 x = make_float3(xp.x, xp.y, xp.z);
+                float3 v = make_float3(vp.x, vp.y, vp.z);
+                const uint32_t n = __float_as_uint(k0.w);
+                const float3 mean = make_float3(k0.x, k0.y, k0.z);
+                bool collided = false;
+                if (ALGO == 0) {
+                    if (n > 1) {
+                        // v' = u + v_par + cos a v_perp + sin a (v_perp x axis), with fused
+                        // multiply-adds (the collision is compared to 1e-5, not bit-exactly)
+                        const float3 axis = make_float3(k1.x, k1.y, k1.z);
+                        const float3 vr = make_float3(v.x - mean.x, v.y - mean.y, v.z - mean.z);
+                        const float vd = __fmaf_rn(vr.x, axis.x, __fmaf_rn(vr.y, axis.y, vr.z * axis.z));
+                        const float3 vpara = make_float3(axis.x * vd, axis.y * vd, axis.z * vd);
+                        const float3 vperp = make_float3(vr.x - vpara.x, vr.y - vpara.y, vr.z - vpara.z);
+                        const float3 cr = make_float3(__fmaf_rn(vperp.y, axis.z, -(vperp.z * axis.y)),
+                                                      __fmaf_rn(vperp.z, axis.x, -(vperp.x * axis.z)),
+                                                      __fmaf_rn(vperp.x, axis.y, -(vperp.y * axis.x)));
+                        v = make_float3(__fmaf_rn(b.sin_a, cr.x, __fmaf_rn(b.cos_a, vperp.x, vpara.x)) + mean.x,
+                                        __fmaf_rn(b.sin_a, cr.y, __fmaf_rn(b.cos_a, vperp.y, vpara.y)) + mean.y,
+                                        __fmaf_rn(b.sin_a, cr.z, __fmaf_rn(b.cos_a, vperp.z, vpara.z)) + mean.z);
+                        x = pbc(b, make_float3(x.x - s.x, x.y - s.y, x.z - s.z));
+                        v.x += b.drag_dt;
+                        collided = true;
+                    }
+                } else {
+                    const float4 k2 = L.omega[ci];
+                    const uint32_t m = __float_as_uint(k2.w);
+                    if (n > 1 && s_rank[p] < m) {
+                        const float3 com = make_float3(k1.x, k1.y, k1.z);
+                        const float3 omega = make_float3(k2.x, k2.y, k2.z);
+                        v.x += mean.x; v.y += mean.y; v.z += mean.z;
+                        v.x += b.drag_dt;
+                        const float3 cr = cross3(x, omega);
+                        v.x -= cr.x; v.y -= cr.y; v.z -= cr.z;
+                        x = pbc(b, make_float3((com.x + x.x) - s.x, (com.y + x.y) - s.y, (com.z + x.z) - s.z));
+                        collided = true;
+                    }
+                }
+                if (REPLAY) {
+                    const uint64_t i3 = 3 * (uint64_t)__float_as_uint(vp.w);
+                    a.dense_pos[i3] = x.x; a.dense_pos[i3 + 1] = x.y; a.dense_pos[i3 + 2] = x.z;
+                    a.dense_vel[i3] = v.x; a.dense_vel[i3 + 1] = v.y; a.dense_vel[i3 + 2] = v.z;
+                    return;
+                }
+                float3 vn = v;
+                const float3 xn = stream_shift(b, x, vn, sn);
+                if (a.pressure) {
+                    // collision in a wall-layer cell: the ghosts took up minus the real
+                    // particles' z momentum change (extended: the leader has subtracted
+                    // the participants' momentum before the collision)
+                    const uint32_t side = __float_as_uint(k1.w);
+                    if (side) {
+                        const float sg = side == 1 ? 1.0f : -1.0f;
+                        if (ALGO == 0) imp[side - 1] += sg * (v.z - vp.z);
+                        else if (collided) imp[side - 1] += sg * v.z;
+                    }
+                    if (b.wall_z && vn.z != v.z) imp[v.z > 0.0f ? 1 : 0] += 2.0f * fabsf(v.z);   // bounce-back
+                }
+                const uint32_t next = b.cell_base + storage_index(b, cell_of_wrapped(b, xn));
+                s_pos[p] = make_float4(xn.x, xn.y, xn.z, __uint_as_float(next));
+                s_vel[p] = make_float4(vn.x, vn.y, vn.z, vp.w);
+                const bool need_lab = a.sample || (ALGO == 0 && a.tape_key);
+                const uint32_t lab = need_lab ? b.cell_base + ref_index(b, cell_of_wrapped(b, x)) : 0u;
+                if (ALGO == 0 && a.tape_key) {
+                    const uint32_t id = __float_as_uint(vp.w);
+                    const bool bounced = vn.x != v.x || vn.y != v.y || vn.z != v.z;
+                    a.tape_key[id] = n > 1 ? b.cell_base + c0 + ci : kTapeNone;
+                    a.tape_lab[id] = lab | (bounced ? kTapeBounce : 0u);
+                }
+                if (a.sample) sample_add(a.samp, lab, v, true);
+            };
+
             if (ALGO == 0) {
+                // SRD: exact velocity sum of each cell (2^-32 fixed point, independent of
+                // bucket order; ghosts included), one group per cell
                 const uint32_t i = my_cell;
                 const uint32_t o = in_sub ? L.off[i] - pbase : 0;
                 const uint32_t n = in_sub ? L.cnt[i] + L.ng[i] : 0;
-                long long sx = 0, sy = 0, sz = 0;   // exact sums in units of 2^-32
+                long long sx = 0, sy = 0, sz = 0;
                 for (uint32_t q = my_j; q < n; q += G) {
                     const float4 vq = s_vel[o + q];
                     sx += __float2ll_rn(vq.x * 4294967296.0f);
@@ -721,189 +801,139 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
                     L.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));   // axis: c1, drawn per tile
                     if (!REPLAY && a.tape_ncell) a.tape_ncell[b.cell_base + c0 + i] = n > 1 ? n : 0u;
                 }
-            } else if (in_sub && leader) {
+            } else {
+                // Extended: the first kExtLanes threads of the cell's group walk the
+                // participants in particle-id order (thread j takes ranks j, j + 4, ...) and
+                // reduce with shuffles in a fixed tree, so the arithmetic does not depend on
+                // the tiling (G >= 4 always: extended tiles hold at most 64 cells); every
+                // lane runs every reduction (idle lanes and cells that do not collide add
+                // zeros), only stores depend on the cell.
+                const bool ext_lane = my_j < (uint32_t)kExtLanes;
                 const uint32_t i = my_cell;
-                const uint32_t o = L.off[i] - pbase, cnt = L.cnt[i], g = L.ng[i];
-                const uint3 cc = storage_coords(b, c0 + i);
+                const uint32_t o = in_sub ? L.off[i] - pbase : 0, cnt = in_sub ? L.cnt[i] : 0;
+                const uint32_t g = in_sub ? L.ng[i] : 0;
+                const uint3 cc = storage_coords(b, c0 + (in_sub ? i : 0));
                 const uint32_t ref = ref_index(b, cc);
-                const uint32_t n = min(cnt + g, b.cap);
-                const uint32_t m = n - g;   // real participants (lowest ids)
-                float3 com = make_float3(0, 0, 0), mean = make_float3(0, 0, 0), omega = make_float3(0, 0, 0);
+                const uint32_t n = in_sub ? min(cnt + g, b.cap) : 0;
+                const uint32_t m = n - min(g, n);   // real participants (lowest ids)
+                const bool live = in_sub && n > 1;
                 uint32_t side = 0;   // wall layer of the cell for the pressure estimator: 1 bottom, 2 top
-                if (!REPLAY && a.pressure && b.wall_z)
+                if (!REPLAY && a.pressure && b.wall_z && in_sub)
                     side = cc.z <= 1u ? 1u : (cc.z + 2u >= (uint32_t)b.L[2] ? 2u : 0u);
-                if (n > 1) {
-                    const float3 centre = cell_centre(b, cc);
-                    float gate;
-                    const float3 axis = D::ext_axis(a, b, step, ref, gate);
-                    auto at = [&](uint32_t k) -> uint32_t { return k < m ? s_inv[o + k] : o + cnt + (k - m); };
-                    float real_vz = 0.0f;
-                    for (uint32_t k = 0; k < n; ++k) {
-                        const uint32_t p = at(k);
-                        const float4 xp = s_pos[p], vp = s_vel[p];
-                        com.x += (xp.x - centre.x); com.y += (xp.y - centre.y); com.z += (xp.z - centre.z);
-                        mean.x += vp.x; mean.y += vp.y; mean.z += vp.z;
-                        if (k < m) real_vz += vp.z;
-                    }
-                    if (side) imp[side - 1] -= (side == 1 ? 1.0f : -1.0f) * real_vz;
-                    const float inv = 1.0f / (float)n;
-                    com = make_float3(com.x * inv + centre.x, com.y * inv + centre.y, com.z * inv + centre.z);
-                    mean = make_float3(mean.x * inv, mean.y * inv, mean.z * inv);
-                    float proj0 = 0.0f;
-                    int size0 = 0;
-                    for (uint32_t k = 0; k < n; ++k) {
-                        const uint32_t p = at(k);
-                        float4 xp = s_pos[p], vp = s_vel[p];
-                        xp.x -= com.x; xp.y -= com.y; xp.z -= com.z;
-                        vp.x -= mean.x; vp.y -= mean.y; vp.z -= mean.z;
-                        s_pos[p] = xp;
-                        s_vel[p] = vp;
-                        if (dot3(make_float3(xp.x, xp.y, xp.z), axis) < 0) {
-                            proj0 += dot3(make_float3(vp.x, vp.y, vp.z), axis);
-                            size0 += 1;
-                        }
-                    }
-                    const int size1 = (int)n - size0;
-                    const float proj1 = -proj0 / (float)size1;
-                    proj0 = proj0 / (float)size0;
-                    const float prob = 1 - expf(0.01f * (proj1 - proj0) * (float)size0 * (float)size1);
-                    if (gate < prob) {
-                        const float t0 = proj1 * ((float)size1 / (float)size0);
-                        const float t1 = proj0 * ((float)size0 / (float)size1);
-                        float mean0 = 0.0f, mean1 = 0.0f;
-                        float I[6] = {0, 0, 0, 0, 0, 0};
-                        float3 dL = make_float3(0, 0, 0);
-                        for (uint32_t k = 0; k < n; ++k) {
-                            const uint32_t p = at(k);
-                            const float4 xp = s_pos[p];
-                            float4 vp = s_vel[p];
-                            const float3 x = make_float3(xp.x, xp.y, xp.z);
-                            float3 v = make_float3(vp.x, vp.y, vp.z);
-                            const bool side = dot3(x, axis) < 0;
-                            const float vr = D::thermal(a, b, step, ref, k) * b.tv;
-                            if (side) mean0 += vr; else mean1 += vr;
-                            const float3 cr = cross3(x, v);
-                            dL.x += cr.x; dL.y += cr.y; dL.z += cr.z;
-                            const float kick = (vr - dot3(v, axis)) + (side ? t0 : t1);
-                            v.x += axis.x * kick; v.y += axis.y * kick; v.z += axis.z * kick;
-                            s_vel[p] = make_float4(v.x, v.y, v.z, vp.w);
-                            const float sx = x.x * x.x, sy = x.y * x.y, sz = x.z * x.z;
-                            I[0] += sy + sz;
-                            I[1] += sx + sz;
-                            I[2] += sx + sy;
-                            I[3] += -x.x * x.y;
-                            I[4] += -x.x * x.z;
-                            I[5] += -x.y * x.z;
-                        }
-                        const float m0 = mean0 / (float)size0, m1 = mean1 / (float)size1;
-                        const float3 vm0 = make_float3(axis.x * m0, axis.y * m0, axis.z * m0);
-                        const float3 vm1 = make_float3(axis.x * m1, axis.y * m1, axis.z * m1);
-                        for (uint32_t k = 0; k < n; ++k) {
-                            const uint32_t p = at(k);
-                            const float4 xp = s_pos[p];
-                            float4 vp = s_vel[p];
-                            const float3 x = make_float3(xp.x, xp.y, xp.z);
-                            const float3 vm = dot3(x, axis) < 0 ? vm0 : vm1;
-                            vp.x -= vm.x; vp.y -= vm.y; vp.z -= vm.z;
-                            s_vel[p] = vp;
-                            const float3 cr = cross3(x, make_float3(vp.x, vp.y, vp.z));
-                            dL.x -= cr.x; dL.y -= cr.y; dL.z -= cr.z;
-                        }
-                        float Ii[6];
-                        sym_inverse(I, 1e-5f, Ii);
-                        omega = make_float3(Ii[0] * dL.x + Ii[3] * dL.y + Ii[4] * dL.z,
-                                            Ii[3] * dL.x + Ii[1] * dL.y + Ii[5] * dL.z,
-                                            Ii[4] * dL.x + Ii[5] * dL.y + Ii[2] * dL.z);
+                const float3 centre = cell_centre(b, cc);
+                float gate = 1.0f;
+                float3 axis = make_float3(0, 0, 1);
+                if (live) axis = D::ext_axis(a, b, step, ref, gate);
+                auto at = [&](uint32_t k) -> uint32_t { return k < m ? s_inv[o + k] : o + cnt + (k - m); };
+                // centre of mass and mean velocity
+                float3 com = make_float3(0, 0, 0), mean = make_float3(0, 0, 0);
+                float real_vz = 0.0f;
+                for (uint32_t k = my_j; ext_lane && live && k < n; k += kExtLanes) {
+                    const uint32_t p = at(k);
+                    const float4 xp = s_pos[p], vp = s_vel[p];
+                    com.x += (xp.x - centre.x); com.y += (xp.y - centre.y); com.z += (xp.z - centre.z);
+                    mean.x += vp.x; mean.y += vp.y; mean.z += vp.z;
+                    if (k < m) real_vz += vp.z;
+                }
+                com = make_float3(group_sum(com.x, kExtLanes), group_sum(com.y, kExtLanes), group_sum(com.z, kExtLanes));
+                mean = make_float3(group_sum(mean.x, kExtLanes), group_sum(mean.y, kExtLanes), group_sum(mean.z, kExtLanes));
+                real_vz = group_sum(real_vz, kExtLanes);
+                if (live && side && leader) imp[side - 1] -= (side == 1 ? 1.0f : -1.0f) * real_vz;
+                const float inv = live ? 1.0f / (float)n : 0.0f;
+                com = make_float3(com.x * inv + centre.x, com.y * inv + centre.y, com.z * inv + centre.z);
+                mean = make_float3(mean.x * inv, mean.y * inv, mean.z * inv);
+                // comoving frame; the side of the plane through the centre of mass
+                float proj0 = 0.0f;
+                int size0 = 0;
+                for (uint32_t k = my_j; ext_lane && live && k < n; k += kExtLanes) {
+                    const uint32_t p = at(k);
+                    float4 xp = s_pos[p], vp = s_vel[p];
+                    xp.x -= com.x; xp.y -= com.y; xp.z -= com.z;
+                    vp.x -= mean.x; vp.y -= mean.y; vp.z -= mean.z;
+                    s_pos[p] = xp;
+                    s_vel[p] = vp;
+                    if (dot3(make_float3(xp.x, xp.y, xp.z), axis) < 0) {
+                        proj0 += dot3(make_float3(vp.x, vp.y, vp.z), axis);
+                        size0 += 1;
                     }
                 }
-                L.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));
-                L.c1[i] = make_float4(com.x, com.y, com.z, __uint_as_float(side));
-                L.omega[i] = make_float4(omega.x, omega.y, omega.z, __uint_as_float(m));
+                proj0 = group_sum(proj0, kExtLanes);
+                size0 = group_sum(size0, kExtLanes);
+                const int size1 = (int)n - size0;
+                const float proj1 = live ? -proj0 / (float)size1 : 0.0f;
+                proj0 = live ? proj0 / (float)size0 : 0.0f;
+                const float prob = live ? 1 - expf(0.01f * (proj1 - proj0) * (float)size0 * (float)size1) : 0.0f;
+                const bool collide = live && gate < prob;
+                // stochastic exchange along the axis, thermalised per side
+                const float t0 = collide ? proj1 * ((float)size1 / (float)size0) : 0.0f;
+                const float t1 = collide ? proj0 * ((float)size0 / (float)size1) : 0.0f;
+                float mean0 = 0.0f, mean1 = 0.0f;
+                float I[6] = {0, 0, 0, 0, 0, 0};
+                float3 dL = make_float3(0, 0, 0);
+                for (uint32_t k = my_j; ext_lane && collide && k < n; k += kExtLanes) {
+                    const uint32_t p = at(k);
+                    const float4 xp = s_pos[p];
+                    float4 vp = s_vel[p];
+                    const float3 x = make_float3(xp.x, xp.y, xp.z);
+                    float3 v = make_float3(vp.x, vp.y, vp.z);
+                    const bool sd = dot3(x, axis) < 0;
+                    const float vr = D::thermal(a, b, step, ref, k) * b.tv;
+                    if (sd) mean0 += vr; else mean1 += vr;
+                    const float3 cr = cross3(x, v);
+                    dL.x += cr.x; dL.y += cr.y; dL.z += cr.z;
+                    const float kick = (vr - dot3(v, axis)) + (sd ? t0 : t1);
+                    v.x += axis.x * kick; v.y += axis.y * kick; v.z += axis.z * kick;
+                    s_vel[p] = make_float4(v.x, v.y, v.z, vp.w);
+                    const float sx = x.x * x.x, sy = x.y * x.y, sz = x.z * x.z;
+                    I[0] += sy + sz;
+                    I[1] += sx + sz;
+                    I[2] += sx + sy;
+                    I[3] += -x.x * x.y;
+                    I[4] += -x.x * x.z;
+                    I[5] += -x.y * x.z;
+                }
+                mean0 = group_sum(mean0, kExtLanes);
+                mean1 = group_sum(mean1, kExtLanes);
+#pragma unroll
+                for (int q = 0; q < 6; ++q) I[q] = group_sum(I[q], kExtLanes);
+                const float m0 = collide ? mean0 / (float)size0 : 0.0f, m1 = collide ? mean1 / (float)size1 : 0.0f;
+                const float3 vm0 = make_float3(axis.x * m0, axis.y * m0, axis.z * m0);
+                const float3 vm1 = make_float3(axis.x * m1, axis.y * m1, axis.z * m1);
+                for (uint32_t k = my_j; ext_lane && collide && k < n; k += kExtLanes) {
+                    const uint32_t p = at(k);
+                    const float4 xp = s_pos[p];
+                    float4 vp = s_vel[p];
+                    const float3 x = make_float3(xp.x, xp.y, xp.z);
+                    const float3 vm = dot3(x, axis) < 0 ? vm0 : vm1;
+                    vp.x -= vm.x; vp.y -= vm.y; vp.z -= vm.z;
+                    s_vel[p] = vp;
+                    const float3 cr = cross3(x, make_float3(vp.x, vp.y, vp.z));
+                    dL.x -= cr.x; dL.y -= cr.y; dL.z -= cr.z;
+                }
+                dL = make_float3(group_sum(dL.x, kExtLanes), group_sum(dL.y, kExtLanes), group_sum(dL.z, kExtLanes));
+                float3 omega = make_float3(0, 0, 0);
+                if (collide) {
+                    float Ii[6];
+                    sym_inverse(I, 1e-5f, Ii);
+                    omega = make_float3(Ii[0] * dL.x + Ii[3] * dL.y + Ii[4] * dL.z,
+                                        Ii[3] * dL.x + Ii[1] * dL.y + Ii[5] * dL.z,
+                                        Ii[4] * dL.x + Ii[5] * dL.y + Ii[2] * dL.z);
+                }
+                if (in_sub && leader) {
+                    L.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));
+                    L.c1[i] = make_float4(com.x, com.y, com.z, __uint_as_float(side));
+                    L.omega[i] = make_float4(omega.x, omega.y, omega.z, __uint_as_float(m));
+                }
             }
             __syncthreads();
-
-            // per particle: finish the collision, sample, find the next cell
+            // particle-parallel finish over the sub-tile
             for (uint32_t pb = 0; pb < np; pb += kThreads) {
                 const uint32_t p = pb + tid;
-                bool active = false;
-                uint32_t ci = 0;
-                if (p < np) {
-                    const uint32_t info = s_cell[p];
-                    ci = info & ~kGhostFlag;
-                    active = !(info & kGhostFlag);
-                }
-                float3 x = make_float3(0, 0, 0), v = make_float3(0, 0, 0);
-                if (active) {
-                    const float4 xp = s_pos[p], vp = s_vel[p];
-                    x = make_float3(xp.x, xp.y, xp.z);
-                    v = make_float3(vp.x, vp.y, vp.z);
-                    const float4 k0 = L.c0[ci], k1 = L.c1[ci];
-                    const uint32_t n = __float_as_uint(k0.w);
-                    const float3 mean = make_float3(k0.x, k0.y, k0.z);
-                    if (ALGO == 0) {
-                        if (n > 1) {
-                            const float3 axis = make_float3(k1.x, k1.y, k1.z);
-                            const float3 vr = make_float3(v.x - mean.x, v.y - mean.y, v.z - mean.z);
-                            const float vd = dot3(vr, axis);
-                            const float3 vpara = make_float3(axis.x * vd, axis.y * vd, axis.z * vd);
-                            const float3 vperp = make_float3(vr.x - vpara.x, vr.y - vpara.y, vr.z - vpara.z);
-                            const float3 cr = cross3(vperp, axis);
-                            v = make_float3((vpara.x + b.cos_a * vperp.x) + b.sin_a * cr.x,
-                                            (vpara.y + b.cos_a * vperp.y) + b.sin_a * cr.y,
-                                            (vpara.z + b.cos_a * vperp.z) + b.sin_a * cr.z);
-                            v.x += mean.x; v.y += mean.y; v.z += mean.z;
-                            x = pbc(b, make_float3(x.x - s.x, x.y - s.y, x.z - s.z));
-                            v.x += b.drag_dt;
-                        }
-                    } else {
-                        const float4 k2 = L.omega[ci];
-                        const uint32_t m = __float_as_uint(k2.w);
-                        if (n > 1 && s_rank[p] < m) {
-                            const float3 com = make_float3(k1.x, k1.y, k1.z);
-                            const float3 omega = make_float3(k2.x, k2.y, k2.z);
-                            v.x += mean.x; v.y += mean.y; v.z += mean.z;
-                            v.x += b.drag_dt;
-                            const float3 cr = cross3(x, omega);
-                            v.x -= cr.x; v.y -= cr.y; v.z -= cr.z;
-                            x = pbc(b, make_float3((com.x + x.x) - s.x, (com.y + x.y) - s.y, (com.z + x.z) - s.z));
-                        }
-                    }
-                    if (REPLAY) {
-                        const uint64_t i3 = 3 * (uint64_t)__float_as_uint(vp.w);
-                        a.dense_pos[i3] = x.x; a.dense_pos[i3 + 1] = x.y; a.dense_pos[i3 + 2] = x.z;
-                        a.dense_vel[i3] = v.x; a.dense_vel[i3 + 1] = v.y; a.dense_vel[i3 + 2] = v.z;
-                    } else {
-                        float3 vn = v;
-                        const float3 xn = stream_shift(b, x, vn, sn);
-                        if (a.pressure) {
-                            // collision in a wall-layer cell: the ghosts took up minus the
-                            // real particles' z momentum change (extended: the leader has
-                            // subtracted the participants' momentum before the collision)
-                            const uint32_t side = __float_as_uint(k1.w);
-                            if (side) {
-                                const float sg = side == 1 ? 1.0f : -1.0f;
-                                if (ALGO == 0) imp[side - 1] += sg * (v.z - vp.z);
-                                else if (n > 1 && s_rank[p] < __float_as_uint(L.omega[ci].w)) imp[side - 1] += sg * v.z;
-                            }
-                            if (b.wall_z && vn.z != v.z) imp[v.z > 0.0f ? 1 : 0] += 2.0f * fabsf(v.z);   // bounce-back
-                        }
-                        const uint32_t next = b.cell_base + storage_index(b, cell_of(b, xn));
-                        s_pos[p] = make_float4(xn.x, xn.y, xn.z, __uint_as_float(next));
-                        s_vel[p] = make_float4(vn.x, vn.y, vn.z, vp.w);
-                        if (ALGO == 0 && a.tape_key) {
-                            const uint32_t id = __float_as_uint(vp.w);
-                            const bool bounced = vn.x != v.x || vn.y != v.y || vn.z != v.z;
-                            a.tape_key[id] = n > 1 ? b.cell_base + c0 + ci : kTapeNone;
-                            a.tape_lab[id] = (b.cell_base + ref_index(b, cell_of(b, x))) | (bounced ? kTapeBounce : 0u);
-                        }
-                    }
-                } else if (p < np) {
-                    reinterpret_cast<uint32_t*>(s_pos + p)[3] = kNoKey;
-                }
-                if (!REPLAY && a.sample) {
-                    const uint32_t lab = active ? b.cell_base + ref_index(b, cell_of(b, x)) : 0;
-                    sample_add(a.samp, lab, v, active);
-                }
+                if (p >= np) continue;
+                const uint32_t info = s_cell[p];
+                const uint32_t ci = info & ~kGhostFlag;
+                if (info & kGhostFlag) reinterpret_cast<uint32_t*>(s_pos + p)[3] = kNoKey;
+                else finish(p, ci, L.c0[ci], L.c1[ci]);
             }
             __syncthreads();
             if (REPLAY) {
@@ -998,7 +1028,7 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(StepArgs a, const flo
             const float3 v0 = vs;
             xs = stream_shift(b, make_float3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), vs,
                               grid_shift(b, bi, a.step + 1, a.state));
-            key = b.cell_base + storage_index(b, cell_of(b, xs));
+            key = b.cell_base + storage_index(b, cell_of_wrapped(b, xs));
             if (a.tape_lab) a.tape_lab[i] = (vs.x != v0.x || vs.y != v0.y || vs.z != v0.z) ? kTapeBounce : 0u;
         }
         store_particle(a, a.boxes[bi], xs, vs, (uint32_t)i, key, active);

@@ -150,6 +150,18 @@ int32_t mpcd_gb_inject_draws(mpcd_gb_handle *h, uint32_t gmax, uint32_t pmax, co
  * [1] error flags (bit 0 overflow list full, bit 1 wait timeout, bit 2 key mismatch). */
 int32_t mpcd_gb_counters(mpcd_gb_handle *h, uint64_t out[2]);
 
+/* ---- snapshots: checkpoint and resume (the reference's writeBackupFile is a TODO,
+ *      src/libmpcd/cuda_backend/cuda_backend_impl.cu:77-79) ---- */
+
+/* Write the handle's state to `path`.  The file holds the step index, every box's
+ * parameters and Philox seed, and the post-step positions and velocities by particle id,
+ * with a checksum.  The layout is in mpcd_engine.cu.  Sample sums are not saved. */
+int32_t mpcd_gb_save_snapshot(mpcd_gb_handle *h, const char *path);
+/* Load a snapshot into a handle created with the same boxes (geometry, n, dt, T,
+ * drag, seed, algorithm; MPCD_GB_EINVAL otherwise).  Stepping on continues the
+ * saved trajectory bit for bit. */
+int32_t mpcd_gb_load_snapshot(mpcd_gb_handle *h, const char *path);
+
 /* ---- batched ensemble (no counterpart in the reference) ---- */
 
 /* R independent boxes advanced together: one step-kernel launch per step walks a
