@@ -591,19 +591,40 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
                 L.c1[i] = make_float4(ax.x, ax.y, ax.z, __uint_as_float(side));
             }
         }
-        // one scan of (particles << 16 | ghosts): a tile holds fewer than 2^16 of either
-        uint32_t packed_total;
-        const uint32_t packed = block_exclusive_scan(((mine + mine_g) << 16) | mine_g, warp_tot, packed_total);
-        next_raw = fetch_count(a, s_next_first, s_next_nc, my_cell, leader);   // after the scan's barriers
-        if (leader && my_cell < nc) {
-            L.off[my_cell] = packed >> 16;
-            L.goff[my_cell] = packed & 0xFFFFu;
-        }
-        if (tid == 0) {
-            L.off[nc] = packed_total >> 16;
-            L.goff[nc] = packed_total & 0xFFFFu;
+        // offsets of the tile's cells: one warp scans (particles << 16 | ghosts) of up
+        // to 128 cells, 4 per lane (a tile holds fewer than 2^16 of either)
+        __syncthreads();
+        if (tid < 32) {
+            uint32_t v[4], run = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t c = 4 * (uint32_t)tid + k;
+                v[k] = c < nc ? ((L.cnt[c] + L.ng[c]) << 16) | L.ng[c] : 0u;
+                run += v[k];
+            }
+            uint32_t incl = run;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t t = __shfl_up_sync(kFull, incl, d);
+                if (tid >= d) incl += t;
+            }
+            uint32_t at = incl - run;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t c = 4 * (uint32_t)tid + k;
+                if (c < nc) {
+                    L.off[c] = at >> 16;
+                    L.goff[c] = at & 0xFFFFu;
+                }
+                at += v[k];
+            }
+            if (tid == 31) {
+                L.off[nc] = incl >> 16;
+                L.goff[nc] = incl & 0xFFFFu;
+            }
         }
         __syncthreads();
+        next_raw = fetch_count(a, s_next_first, s_next_nc, my_cell, leader);
 
         // sub-tiles of consecutive cells whose particles fit the buffer
         uint32_t i0 = 0;
@@ -781,13 +802,26 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
                 const uint32_t i = my_cell;
                 const uint32_t o = in_sub ? L.off[i] - pbase : 0;
                 const uint32_t n = in_sub ? L.cnt[i] + L.ng[i] : 0;
-                long long sx = 0, sy = 0, sz = 0;
-                for (uint32_t q = my_j; q < n; q += G) {
-                    const float4 vq = s_vel[o + q];
-                    sx += __float2ll_rn(vq.x * 4294967296.0f);
-                    sy += __float2ll_rn(vq.y * 4294967296.0f);
-                    sz += __float2ll_rn(vq.z * 4294967296.0f);
+                long long sx = 0, sy = 0, sz = 0, tx = 0, ty = 0, tz = 0;   // two chains (integer: exact)
+                uint32_t q = my_j;
+                for (; q + G < n; q += 2 * G) {
+                    const float4 va = s_vel[o + q], vb = s_vel[o + q + G];
+                    sx += __float2ll_rn(va.x * 4294967296.0f);
+                    sy += __float2ll_rn(va.y * 4294967296.0f);
+                    sz += __float2ll_rn(va.z * 4294967296.0f);
+                    tx += __float2ll_rn(vb.x * 4294967296.0f);
+                    ty += __float2ll_rn(vb.y * 4294967296.0f);
+                    tz += __float2ll_rn(vb.z * 4294967296.0f);
                 }
+                if (q < n) {
+                    const float4 va = s_vel[o + q];
+                    sx += __float2ll_rn(va.x * 4294967296.0f);
+                    sy += __float2ll_rn(va.y * 4294967296.0f);
+                    sz += __float2ll_rn(va.z * 4294967296.0f);
+                }
+                sx += tx;
+                sy += ty;
+                sz += tz;
                 sx = group_sum(sx, G);
                 sy = group_sum(sy, G);
                 sz = group_sum(sz, G);
