@@ -137,6 +137,25 @@ def ncu_traffic_per_particle():
         return None, None
 
 
+# ---------------------------------------------------------------- ranks
+
+def reduce_max(x: float, dist=None, device: str = "cuda") -> float:
+    """x maximised over the ranks of the process group (the slowest rank's time);
+    x itself without a process group."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world: int, particles_per_rank: int, steps: int, elapsed_s: float) -> float:
+    """Particle-steps/s of the whole job: every rank advances its own replica."""
+    return world * particles_per_rank * steps / elapsed_s
+
+
 # ---------------------------------------------------------------- CPU (oracle) timing
 
 def cpu_rate(threads: int, warmup: int, steps: int):
@@ -195,8 +214,6 @@ def run_e2e(args, wl, algorithm, rank, local_rank, dist, world, N):
     """Same metric through the Python API the reference exposes: a fresh
     Simulation, step_and_sample over the timed steps and get_mean_fields (the
     device-to-host read of the result), host wall clock."""
-    import torch
-
     import cudampcd_gb300 as pympcd
 
     params = pympcd.Params()
@@ -217,13 +234,9 @@ def run_e2e(args, wl, algorithm, rank, local_rank, dist, world, N):
     t0 = time.perf_counter()
     sim.step_and_sample(args.steps)
     density, velocity = sim.get_mean_fields()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = reduce_max(time.perf_counter() - t0, dist)
     del sim
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * N * args.steps / e2e_s
+    e2e_value = whole_job_rate(world, N, args.steps, e2e_s)
     d2h = (density.nbytes + velocity.nbytes) / args.steps
     return {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,
             "api": "cudampcd_gb300.Simulation.step_and_sample + get_mean_fields (host wall clock)"}
@@ -263,12 +276,8 @@ def run_gpu_arm(args, rank, world, local_rank):
     torch.cuda.synchronize()
     overflowed, flags = h.counters()
     h.close()
-    elapsed = total_ms
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
-    value = world * N * args.steps / (elapsed * 1e-3)
+    elapsed = reduce_max(total_ms, dist)
+    value = whole_job_rate(world, N, args.steps, elapsed * 1e-3)
 
     # end to end through the Python API: step_and_sample + get_mean_fields
     e2e = None
