@@ -87,6 +87,15 @@ __device__ __forceinline__ float pbc1_fast(float a, float L, float L2)
     return a - (a >= L2 ? L2 : (a >= L ? L : 0.0f));
 }
 
+// The general (fmodf) path of pbc for arguments far outside the box; kept out of
+// line so the hot loops stay small.
+__device__ __noinline__ float3 pbc_general(const BoxDesc& b, float3 r)
+{
+    return make_float3(pbc1(r.x, b.Lf[0], b.L15[0], b.L2x[0], b.L3x[0], b.Lh[0]),
+                       pbc1(r.y, b.Lf[1], b.L15[1], b.L2x[1], b.L3x[1], b.Lh[1]),
+                       pbc1(r.z, b.Lf[2], b.L15[2], b.L2x[2], b.L3x[2], b.Lh[2]));
+}
+
 // All three axes; one branch to the fmodf path when any a = r + 1.5L leaves [0, 3L).
 __device__ __forceinline__ float3 pbc(const BoxDesc& b, float3 r)
 {
@@ -95,9 +104,7 @@ __device__ __forceinline__ float3 pbc(const BoxDesc& b, float3 r)
     if (__builtin_expect(in, 1))
         return make_float3(pbc1_fast(ax, b.Lf[0], b.L2x[0]) - b.Lh[0], pbc1_fast(ay, b.Lf[1], b.L2x[1]) - b.Lh[1],
                            pbc1_fast(az, b.Lf[2], b.L2x[2]) - b.Lh[2]);
-    return make_float3(pbc1(r.x, b.Lf[0], b.L15[0], b.L2x[0], b.L3x[0], b.Lh[0]),
-                       pbc1(r.y, b.Lf[1], b.L15[1], b.L2x[1], b.L3x[1], b.Lh[1]),
-                       pbc1(r.z, b.Lf[2], b.L15[2], b.L2x[2], b.L3x[2], b.Lh[2]));
+    return pbc_general(b, r);
 }
 
 // Coordinate of a cell along one axis: floor(x + L/2) mod L, with the

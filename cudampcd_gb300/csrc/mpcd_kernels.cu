@@ -491,6 +491,7 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
     __shared__ uint64_t bar;
     __shared__ BoxDesc sbox;
     __shared__ int sbox_index;
+    __shared__ uint32_t s_armed;   // the tile's copies were armed by the scan warp
     __shared__ float3 sshift[2];
     const uint32_t tcells = a.boxes_tile_cells;   // cells per tile, the same for every box of the launch
     const TileLayout L = carve(dyn, pbuf, tcells, ALGO);
@@ -538,7 +539,7 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
                 sshift[1] = grid_shift(*bp, bi, step + 1, a.state);
             }
         }
-        __syncthreads();
+        if (!SINGLE || tile == blockIdx.x) __syncthreads();   // a single box never changes after the first tile
         // single box: geometry straight from the kernel parameters (constant bank)
         const BoxDesc& b = SINGLE ? a.box0 : sbox;
         const uint32_t c0 = (tile - b.tile_base) * b.tile_cells;
@@ -621,6 +622,14 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
             if (tid == 31) {
                 L.off[nc] = incl >> 16;
                 L.goff[nc] = incl & 0xFFFFu;
+                // the whole tile fits the buffer (the common case): arm its copies here,
+                // which spares the sub-tile loop a barrier
+                const uint32_t total = incl >> 16, real = total - (incl & 0xFFFFu);
+                s_armed = total <= pbuf;
+                if (total <= pbuf && real) {
+                    fence_proxy_async();
+                    mbar_arrive_expect_tx(&bar, 32u * real);
+                }
             }
         }
         __syncthreads();
@@ -645,11 +654,13 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
 
             // stage real particles: one bulk copy per cell and array
             const uint32_t real_bytes = 32u * (np - (L.goff[i1] - L.goff[i0]));
-            if (tid == 0 && real_bytes) {
-                fence_proxy_async();
-                mbar_arrive_expect_tx(&bar, real_bytes);
+            if (!(s_armed && i0 == 0)) {   // not armed by the scan warp: this sub-tile arms its own
+                if (tid == 0 && real_bytes) {
+                    fence_proxy_async();
+                    mbar_arrive_expect_tx(&bar, real_bytes);
+                }
+                __syncthreads();
             }
-            __syncthreads();
             const bool in_sub = my_cell >= i0 && my_cell < i1;
             if (in_sub) {
                 const uint32_t i = my_cell;
@@ -969,14 +980,16 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
                 if (info & kGhostFlag) reinterpret_cast<uint32_t*>(s_pos + p)[3] = kNoKey;
                 else finish(p, ci, L.c0[ci], L.c1[ci]);
             }
-            __syncthreads();
             if (REPLAY) {
+                __syncthreads();
                 i0 = i1;
                 continue;
             }
 
             // claim bucket slots (warp-aggregated atomics, all issued before any
-            // result is used), then write the particles to their buckets
+            // result is used), then write the particles to their buckets; each
+            // thread claims the entries p = tid + 256 j it finished itself, so no
+            // barrier separates the two passes
             {
                 uint32_t key[kMaxPerThread], peers[kMaxPerThread], base[kMaxPerThread];
                 const int jmax = (int)((np + kThreads - 1) / kThreads);   // the same for every thread
