@@ -6,8 +6,8 @@ import numpy as np
 import oracle as O
 from cudampcd_gb300 import capi
 
-# Tolerance of the floating-point parity checks: the benchmark spec's bound of 1e-5,
-# relative to max(|v|, thermal velocity) per component.
+# Tolerance of the floating-point parity checks: 1e-5 relative to
+# max(|v|, thermal velocity) per component.
 REL_TOL = 1e-5
 
 
