@@ -104,13 +104,13 @@ public:
     Engine(const mpcd_gb_params* ps, int R) : params_(ps[0]), box_params_(ps, ps + R)
     {
         validate();
+        build_boxes();   // host-side sizes and limits, before any CUDA call
         check(cudaSetDevice((int)params_.device_id), "cudaSetDevice");
         check(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking), "cudaStreamCreate");
         stream_ = own_stream_;
         cudaDeviceProp prop;
         check(cudaGetDeviceProperties(&prop, (int)params_.device_id), "cudaGetDeviceProperties");
         sms_ = prop.multiProcessorCount;
-        build_boxes();
         allocate();
         configure();
         initialise();
