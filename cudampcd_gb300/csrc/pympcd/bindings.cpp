@@ -93,7 +93,7 @@ PYBIND11_MODULE(_pympcd, m)
                 }
                 return vectors_to_numpy(std::move(out));
             },
-            "Particle positions, (N, 3) float32, grouped by cell.")
+            "Particle positions, (N, 3) float32, by particle id (a fixed order).")
         .def(
             "get_particle_velocities",
             [](SimulationHandle const& self) {
@@ -104,7 +104,7 @@ PYBIND11_MODULE(_pympcd, m)
                 }
                 return vectors_to_numpy(std::move(out));
             },
-            "Particle velocities, (N, 3) float32, in the order of get_particle_positions.")
+            "Particle velocities, (N, 3) float32, by particle id.")
         .def(
             "set_particle_positions",
             [](SimulationHandle& self, py::array_t<float, py::array::c_style | py::array::forcecast> a) {
