@@ -915,14 +915,35 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
                 float mean0 = 0.0f, mean1 = 0.0f;
                 float I[6] = {0, 0, 0, 0, 0, 0};
                 float3 dL = make_float3(0, 0, 0);
-                for (uint32_t k = my_j; ext_lane && collide && k < n; k += kExtLanes) {
+                // Thermal draws: participant k uses Gaussian k & 3 of Philox block k >> 2.
+                // With Philox draws, lane j of the group computes block 4u + j once per four
+                // passes (all four Gaussians) and the group exchanges them by shuffles; the
+                // trip count is uniform within the group so every shuffle is collective.
+                const uint32_t passes = (ext_lane && collide) ? (n + kExtLanes - 1) / kExtLanes : 0u;
+                const unsigned gmask = 0xFu << (lane & ~3);   // the cell's 4 collision lanes
+                float gq[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                for (uint32_t t = 0; t < passes; ++t) {
+                    const uint32_t k = kExtLanes * t + my_j;
+                    float gk = 0.0f;
+                    if (!TABLE) {
+                        if ((t & 3u) == 0) {
+                            const uint4 o = draw(b, step, kThermal, ref, t + my_j);
+                            box_muller(o.x, o.y, gq[0], gq[1]);
+                            box_muller(o.z, o.w, gq[2], gq[3]);
+                        }
+                        const int src = (lane & ~3) + (int)(t & 3u);   // the lane holding block t
+                        const float q0 = __shfl_sync(gmask, gq[0], src), q1 = __shfl_sync(gmask, gq[1], src);
+                        const float q2 = __shfl_sync(gmask, gq[2], src), q3 = __shfl_sync(gmask, gq[3], src);
+                        gk = my_j == 0 ? q0 : my_j == 1 ? q1 : my_j == 2 ? q2 : q3;
+                    }
+                    if (k >= n) continue;
                     const uint32_t p = at(k);
                     const float4 xp = s_pos[p];
                     float4 vp = s_vel[p];
                     const float3 x = make_float3(xp.x, xp.y, xp.z);
                     float3 v = make_float3(vp.x, vp.y, vp.z);
                     const bool sd = dot3(x, axis) < 0;
-                    const float vr = D::thermal(a, b, step, ref, k) * b.tv;
+                    const float vr = (TABLE ? D::thermal(a, b, step, ref, k) : gk) * b.tv;
                     if (sd) mean0 += vr; else mean1 += vr;
                     const float3 cr = cross3(x, v);
                     dL.x += cr.x; dL.y += cr.y; dL.z += cr.z;
