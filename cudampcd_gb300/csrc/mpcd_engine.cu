@@ -687,8 +687,9 @@ public:
         out[3] = b.C;
     }
 
-    // Time `steps` real steps of every admissible (tile cells, buffer) pair and
-    // keep the fastest; the steps advance the simulation like any others.
+    // Time `steps` real steps of every admissible (buffer, fill factor) pair --
+    // each box then takes its own tile size -- and keep the fastest; the steps
+    // advance the simulation like any others.
     void autotune(int steps, uint32_t out[2])
     {
         if (steps < 1) throw Error(MPCD_GB_EINVAL, "autotune needs at least one step per candidate");
@@ -698,12 +699,17 @@ public:
         check(cudaEventCreate(&e0), "event");
         check(cudaEventCreate(&e1), "event");
         float best = -1.0f;
-        uint32_t best_tc = boxes_[0].tile_cells, best_pbuf = pbuf_;
+        double best_fill = fill_;
+        uint32_t best_pbuf = pbuf_;
+        std::vector<std::vector<uint32_t>> tried;   // tilings already timed (per-box tile cells + buffer)
         for (uint32_t pbuf : {1024u, 1536u, 2048u}) {
             if (pbuf < 5 * n_max) continue;
-            for (uint32_t tc = 8; tc <= (params_.algorithm == 1 ? 64u : 128u); tc <<= 1) {
-                if (tc * n_max > pbuf) continue;
-                retile(tc, pbuf);
+            for (double fill : {1.0, 1.15, 1.3, 1.6, 2.0, 3.0}) {
+                std::vector<uint32_t> key{pbuf};
+                for (const BoxDesc& b : boxes_) key.push_back(tile_for(b.n, fill, pbuf));
+                if (std::find(tried.begin(), tried.end(), key) != tried.end()) continue;
+                tried.push_back(key);
+                retile(fill, pbuf);
                 launch_one_step(false);   // first launch of a configuration: not timed
                 check(cudaEventRecord(e0, stream_), "event");
                 for (int i = 0; i < steps; ++i) launch_one_step(false);
@@ -714,15 +720,15 @@ public:
                 check_device_errors();
                 if (best < 0 || ms < best) {
                     best = ms;
-                    best_tc = tc;
+                    best_fill = fill;
                     best_pbuf = pbuf;
                 }
             }
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        retile(best_tc, best_pbuf);
-        out[0] = best_tc;
+        retile(best_fill, best_pbuf);
+        out[0] = max_tile_cells_;
         out[1] = best_pbuf;
     }
 
@@ -819,15 +825,11 @@ private:
         ov_cap_ = (uint32_t)std::max<uint64_t>(1u << 16, std::min<uint64_t>(N_, 1u << 22));
         if (total_slots_ + ov_cap_ >= (1ull << 32))
             throw Error(MPCD_GB_EINVAL, "cells * 4n exceeds the 32-bit slot space of one handle");
-        // tile: a power-of-two number of cells (a group of 256 / cells threads per
-        // cell), about 1300 particles; the buffer holds one cell with all its
-        // ghosts (cap + n = 5n) at least
+        // tiles: per box a power-of-two number of cells (a group of 256 / cells
+        // threads per cell) holding about pbuf / 1.15 particles; the buffer holds
+        // one cell with all its ghosts (cap + n = 5n) at least
         uint32_t pbuf = std::max(1536u, 5 * n_max);
         if (pbuf > 2048) throw Error(MPCD_GB_EINVAL, "n above 409: one cell and its ghosts must fit a tile");
-        // extended: at least 4 threads per cell (its fixed 4-lane reductions)
-        const uint32_t tc_max = params_.algorithm == 1 ? 64u : 128u;
-        uint32_t tc = tc_max;
-        while (tc > 8 && tc * n_max * 1.15 > pbuf) tc >>= 1;
         // tuning overrides (used by the tuning sweeps)
         if (const char* e = std::getenv("MPCD_GB_PBUF")) {
             const uint32_t v = (uint32_t)std::strtoul(e, nullptr, 10);
@@ -835,9 +837,9 @@ private:
         }
         if (const char* e = std::getenv("MPCD_GB_TILE_CELLS")) {
             const uint32_t v = (uint32_t)std::strtoul(e, nullptr, 10);
-            if (v >= 8 && v <= tc_max && (v & (v - 1)) == 0) tc = v;
+            if (v >= 8 && v <= tile_cells_max() && (v & (v - 1)) == 0) forced_tile_cells_ = v;
         }
-        set_tiles(tc, pbuf);
+        set_tiles(1.15, pbuf);
         float table[13][3];
         const int steps = 4;
         for (int select = 0; select <= 12; ++select) {   // simulation_functions.cpp:272-290
@@ -855,35 +857,66 @@ private:
         std::memcpy(ext_axis_, table, sizeof table);
     }
 
+    // extended: at least 4 threads per cell (its fixed 4-lane reductions); the
+    // offset scan covers 128 cells
+    uint32_t tile_cells_max() const { return params_.algorithm == 1 ? 64u : 128u; }
+
+    // Tile of a box of density n: the largest power of two (8 .. tile_cells_max)
+    // whose expected particles, tc * n * fill, fit the buffer.  Sparse boxes of an
+    // ensemble so take larger tiles than dense ones.
+    uint32_t tile_for(uint32_t n, double fill, uint32_t pbuf) const
+    {
+        if (forced_tile_cells_) return forced_tile_cells_;
+        uint32_t tc = tile_cells_max();
+        while (tc > 8 && tc * n * fill > pbuf) tc >>= 1;
+        return tc;
+    }
+
     // Work decomposition only: buckets are per cell, so tiles can change between steps.
-    void set_tiles(uint32_t tc, uint32_t pbuf)
+    void set_tiles(double fill, uint32_t pbuf)
     {
         uint64_t tiles = 0;
-        for (BoxDesc& b : boxes_) {
+        max_tile_cells_ = 0;
+        tile_info_.clear();
+        for (size_t r = 0; r < boxes_.size(); ++r) {
+            BoxDesc& b = boxes_[r];
+            const uint32_t tc = tile_for(b.n, fill, pbuf);
             b.tile_cells = tc;
             b.tile_base = (uint32_t)tiles;
             b.tiles = (b.C + tc - 1) / tc;
             tiles += b.tiles;
+            max_tile_cells_ = std::max(max_tile_cells_, tc);
+            for (uint32_t t = 0; t < b.tiles; ++t)
+                tile_info_.push_back({b.cell_base + t * tc, std::min(tc, b.C - t * tc) | (tc << 16), (uint32_t)r, 0u});
         }
         tiles_ = tiles;
         pbuf_ = pbuf;
+        fill_ = fill;
         for (auto& g : graph_) g.reset();   // graphs bake the tiling into their launches
     }
 
-    void retile(uint32_t tc, uint32_t pbuf)
+    void retile(double fill, uint32_t pbuf)
     {
         check(cudaStreamSynchronize(stream_), "retile");
-        set_tiles(tc, pbuf);
+        set_tiles(fill, pbuf);
+        upload_tiling();
+        configure();
+    }
+
+    // Box descriptors and the tile table to the device (the stream is idle).
+    void upload_tiling()
+    {
         check(cudaMemcpy(boxes_d_.p, boxes_.data(), sizeof(BoxDesc) * boxes_.size(), cudaMemcpyHostToDevice),
               "upload boxes");
-        configure();
+        const size_t bytes = sizeof(TileEntry) * tile_info_.size();
+        if (tile_info_d_.bytes < bytes) check(tile_info_d_.alloc(bytes), "alloc tile table");
+        check(cudaMemcpy(tile_info_d_.p, tile_info_.data(), bytes, cudaMemcpyHostToDevice), "upload tile table");
     }
 
     void allocate()
     {
         check(boxes_d_.alloc(sizeof(BoxDesc) * boxes_.size()), "alloc boxes");
-        check(cudaMemcpy(boxes_d_.p, boxes_.data(), sizeof(BoxDesc) * boxes_.size(), cudaMemcpyHostToDevice),
-              "upload boxes");
+        upload_tiling();
         for (int k = 0; k < 2; ++k) {
             check(pos_[k].alloc(sizeof(float4) * total_slots_), "alloc bucket positions");
             check(vel_[k].alloc(sizeof(float4) * total_slots_), "alloc bucket velocities");
@@ -911,7 +944,7 @@ private:
     void configure()
     {
         int per_sm = 0;
-        check(configure_step(params_.algorithm, pbuf_, boxes_[0].tile_cells, &per_sm), "configure step kernel");
+        check(configure_step(params_.algorithm, pbuf_, max_tile_cells_, &per_sm), "configure step kernel");
         if (per_sm < 1) throw Error(MPCD_GB_ECUDA, "step kernel does not fit on an SM");
         grid_ = (int)std::min<uint64_t>(tiles_, (uint64_t)sms_ * per_sm);
     }
@@ -956,8 +989,9 @@ private:
         a.box0 = boxes_[0];
         a.boxes = boxes_d_.as<BoxDesc>();
         a.nboxes = (int)boxes_.size();
-        a.boxes_tile_cells = boxes_[0].tile_cells;
+        a.boxes_tile_cells = max_tile_cells_;
         a.num_tiles = (uint32_t)tiles_;
+        a.tile_info = tile_info_d_.as<TileEntry>();
         a.total_slots = total_slots_;
         a.step = k;
         const unsigned p = (unsigned)(k & 1), q = p ^ 1u;
@@ -1210,6 +1244,8 @@ private:
     std::vector<BoxDesc> boxes_;
     uint64_t N_ = 0, cells_ = 0, tiles_ = 0, total_slots_ = 0;
     uint32_t ov_cap_ = 0, pbuf_ = 0;
+    uint32_t max_tile_cells_ = 0, forced_tile_cells_ = 0;   // largest tile of any box; a tile size forced for all
+    double fill_ = 1.15;                                     // expected particles per tile = pbuf / fill
     float ext_axis_[13][3];
     uint64_t step_ = 0;
     bool sampling_ = false;
@@ -1221,6 +1257,8 @@ private:
     int inject_valid_[kMaxInjectedShifts] = {0, 0, 0, 0};
     uint64_t inject_step_[kMaxInjectedShifts] = {0, 0, 0, 0};
     float inject_shift_[kMaxInjectedShifts][3] = {};
+    std::vector<TileEntry> tile_info_;   // tile table of the current tiling
+    DeviceBuffer tile_info_d_;
     DeviceBuffer boxes_d_, pos_[2], vel_[2], count_[3], ov_pos_[2], ov_vel_[2], state_, samp_, acc_, dense_pos_,
         dense_vel_, offsets_, scan_status_, scan_counter_, partial_;
     DeviceBuffer t_count_, t_gpos_, t_gvel_, t_axis_, t_gate_, t_gauss_;

@@ -137,17 +137,6 @@ __device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_tot, uint32_
     return excl;
 }
 
-__device__ __forceinline__ const BoxDesc* find_box(const StepArgs& a, uint32_t tile, int& index)
-{
-    int lo = 0, hi = a.nboxes - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (a.boxes[mid].tile_base <= tile) lo = mid; else hi = mid - 1;
-    }
-    index = lo;
-    return &a.boxes[lo];
-}
-
 __device__ __forceinline__ int box_of_particle(const BoxDesc* boxes, int nboxes, uint64_t id)
 {
     int lo = 0, hi = nboxes - 1;
@@ -397,18 +386,18 @@ __device__ inline TileLayout carve(unsigned char* base, uint32_t pbuf, uint32_t 
     return t;
 }
 
-// First global cell and cell count of `tile`, and its box (one thread per CTA).
+// Entry of `tile`: {first global cell, cells | tile cells << 16, box, 0}; past
+// the last tile {0, tile cells of the launch << 16, 0, 0}.  A single box computes
+// it from the kernel parameters; an ensemble reads the host-built table (one
+// load instead of a search over the boxes).
 template <bool SINGLE>
-__device__ __forceinline__ void locate_tile(const StepArgs& a, uint32_t tile, uint32_t& first, uint32_t& nc, int& bi)
+__device__ __forceinline__ uint4 tile_entry(const StepArgs& a, uint32_t tile)
 {
-    bi = 0;
-    first = 0;
-    nc = 0;
-    if (tile >= a.num_tiles) return;
-    const BoxDesc* bp = SINGLE ? &a.box0 : find_box(a, tile, bi);
-    const uint32_t c0 = (tile - bp->tile_base) * bp->tile_cells;
-    first = bp->cell_base + c0;
-    nc = min(bp->tile_cells, bp->C - c0);
+    if (tile >= a.num_tiles) return make_uint4(0u, a.boxes_tile_cells << 16, 0u, 0u);
+    if (!SINGLE) return __ldg(reinterpret_cast<const uint4*>(a.tile_info) + tile);
+    const BoxDesc& b = a.box0;
+    const uint32_t c0 = tile * b.tile_cells;
+    return make_uint4(b.cell_base + c0, min(b.tile_cells, b.C - c0) | (b.tile_cells << 16), 0u, 0u);
 }
 
 // Count of cell `c` of a tile (first thread of the cell's group); issued one
@@ -472,6 +461,9 @@ __device__ void overflow_pass(const StepArgs& a, uint64_t step)
 
 constexpr int kExtLanes = 4;   // lanes per cell of the extended collision (tiles of <= 64 cells)
 
+// log2 of the threads per cell, G = 256 / tile cells (tile cells a power of two, 8..128).
+__device__ __forceinline__ uint32_t group_log2(uint32_t tile_cells) { return 8u - (31u - __clz(tile_cells)); }
+
 // Sum over the G lanes of a cell group (G a power of two dividing 32).
 template <class T>
 __device__ __forceinline__ T group_sum(T v, uint32_t G)
@@ -489,11 +481,10 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
     extern __shared__ __align__(128) unsigned char dyn[];
     __shared__ uint32_t warp_tot[kThreads / 32 + 1];
     __shared__ uint64_t bar;
-    __shared__ BoxDesc sbox;
-    __shared__ int sbox_index;
+    __shared__ __align__(16) BoxDesc sbox;
     __shared__ uint32_t s_armed;   // the tile's copies were armed by the scan warp
     __shared__ float3 sshift[2];
-    const uint32_t tcells = a.boxes_tile_cells;   // cells per tile, the same for every box of the launch
+    const uint32_t tcells = a.boxes_tile_cells;   // the largest tile of the launch (boxes may use smaller ones)
     const TileLayout L = carve(dyn, pbuf, tcells, ALGO);
     float4* const s_pos = L.pos;
     float4* const s_vel = L.vel;
@@ -503,10 +494,7 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
 
     const int tid = threadIdx.x;
     const int lane = tid & 31;
-    if (tid == 0) {
-        mbar_init(&bar);
-        sbox_index = -1;
-    }
+    if (tid == 0) mbar_init(&bar);
     __syncthreads();
     uint32_t phase = 0;
     const uint64_t step = a.step_base ? *a.step_base + a.step : a.step;   // graph replays read the base
@@ -517,33 +505,45 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
         overflow_pass(a, step);
     }
 
-    // group of G threads per cell (every box of a launch has the same tile size)
-    const uint32_t G = kThreads / tcells;
-    const uint32_t my_cell = (uint32_t)tid / G, my_j = (uint32_t)tid % G;
-    const bool leader = my_j == 0;
-
-    // the tile after the current one: located by one thread, read by the cell leaders
-    __shared__ uint32_t s_next_first, s_next_nc;
-    __shared__ int s_next_box;
-    if (tid == 0) locate_tile<SINGLE>(a, blockIdx.x, s_next_first, s_next_nc, s_next_box);
+    // the tile after the current one (tile_entry): its entry is read by one
+    // thread (kLocator) while the current tile's ghosts are counted, its counts by
+    // the cell leaders after the scan (a group of G = 256 / tile cells threads per
+    // cell; a box's tile size sets G).  Two entries alternate, so that the write
+    // for the next tile never meets a read of the current one.
+    constexpr int kLocator = 64;   // warp 2: not the scan warp, not the box-switch threads
+    __shared__ uint4 s_next[2];
+    if (tid == kLocator) s_next[0] = tile_entry<SINGLE>(a, blockIdx.x);
     __syncthreads();
-    uint32_t next_raw = fetch_count(a, s_next_first, s_next_nc, my_cell, leader);
-    for (uint32_t tile = blockIdx.x; tile < a.num_tiles; tile += gridDim.x) {
-        if (tid == 0) {
-            const int bi = s_next_box;   // located while the previous tile was processed
-            const BoxDesc* bp = SINGLE ? &a.box0 : &a.boxes[bi];
-            if (bi != sbox_index) {   // box and its grid shifts change only between boxes
-                if (!SINGLE) sbox = *bp;
-                sbox_index = bi;
-                sshift[0] = grid_shift(*bp, bi, step, a.state);
-                sshift[1] = grid_shift(*bp, bi, step + 1, a.state);
-            }
+    uint32_t next_raw;
+    {
+        const uint32_t lg = group_log2(s_next[0].y >> 16);
+        next_raw = fetch_count(a, s_next[0].x, s_next[0].y & 0xFFFFu, (uint32_t)tid >> lg, (tid & ((1 << lg) - 1)) == 0);
+    }
+    int cur_box = -1;   // box of the previous tile (every thread keeps the same value)
+    uint32_t par = 0;   // s_next[par]: the current tile's entry
+    for (uint32_t tile = blockIdx.x; tile < a.num_tiles; tile += gridDim.x, par ^= 1u) {
+        const int bi = SINGLE ? 0 : (int)s_next[par].z;   // located while the previous tile was processed
+        if (bi != cur_box) {   // box and its grid shifts change only between boxes: copy and
+            cur_box = bi;      // draw them on separate warps
+            const BoxDesc* bp = SINGLE ? &a.box0 : a.boxes + bi;
+            if (!SINGLE && tid < (int)(sizeof(BoxDesc) / 16))
+                reinterpret_cast<uint4*>(&sbox)[tid] = __ldg(reinterpret_cast<const uint4*>(bp) + tid);
+            if (tid == 32) sshift[0] = grid_shift(*bp, bi, step, a.state);
+            if (tid == 96) sshift[1] = grid_shift(*bp, bi, step + 1, a.state);
+            __syncthreads();
         }
-        if (!SINGLE || tile == blockIdx.x) __syncthreads();   // a single box never changes after the first tile
         // single box: geometry straight from the kernel parameters (constant bank)
         const BoxDesc& b = SINGLE ? a.box0 : sbox;
+        const uint32_t lgG = group_log2(b.tile_cells);
+        const uint32_t G = 1u << lgG;   // threads per cell of this box's tiles
+        const uint32_t my_cell = (uint32_t)tid >> lgG, my_j = (uint32_t)tid & (G - 1u);
+        const bool leader = my_j == 0;
         const uint32_t c0 = (tile - b.tile_base) * b.tile_cells;
         const uint32_t nc = min(b.tile_cells, b.C - c0);
+        // the next tile's entry: loaded here, stored to shared memory after the
+        // ghost counts (its readers all passed the previous tile's last barrier)
+        uint4 next_entry = make_uint4(0u, 0u, 0u, 0u);
+        if (tid == kLocator) next_entry = tile_entry<SINGLE>(a, tile + gridDim.x);
         const float3 s = sshift[0];
         const float3 sn = sshift[1];
         const float shift_abs = fabsf(s.z);
@@ -580,7 +580,7 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
                 L.ng[my_cell] = mine_g;
             }
         }
-        if (tid == 0) locate_tile<SINGLE>(a, tile + gridDim.x, s_next_first, s_next_nc, s_next_box);
+        if (tid == kLocator) s_next[par ^ 1u] = next_entry;
         // SRD rotation axes (and the wall side for the pressure estimator) of the
         // tile's cells, one thread per cell; read after the scan's barriers
         if (ALGO == 0) {
@@ -633,7 +633,11 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
             }
         }
         __syncthreads();
-        next_raw = fetch_count(a, s_next_first, s_next_nc, my_cell, leader);
+        {
+            const uint4 e = s_next[par ^ 1u];
+            const uint32_t lg = group_log2(e.y >> 16);   // the next tile's groups
+            next_raw = fetch_count(a, e.x, e.y & 0xFFFFu, (uint32_t)tid >> lg, (tid & ((1 << lg) - 1)) == 0);
+        }
 
         // sub-tiles of consecutive cells whose particles fit the buffer
         uint32_t i0 = 0;

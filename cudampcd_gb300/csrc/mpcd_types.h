@@ -47,6 +47,17 @@ struct BoxDesc {
     uint32_t seed_lo, seed_hi;
 };
 
+// The step kernel copies a box descriptor into shared memory 16 bytes per thread.
+static_assert(sizeof(BoxDesc) % 16 == 0, "BoxDesc must be a whole number of 16-byte words");
+
+// One tile of an ensemble launch (host-built table, read as one 16-byte load).
+struct alignas(16) TileEntry {
+    uint32_t first;   // first global cell (storage order)
+    uint32_t cells;   // cells of this tile | cells per tile of its box << 16
+    uint32_t box;
+    uint32_t unused;
+};
+
 // FP64 running sums of the lab-grid sample of one cell.
 struct alignas(32) SampleAcc {
     double n, vx, vy, vz;
@@ -86,7 +97,8 @@ struct StepArgs {
     BoxDesc box0;                 // the only box of a single-box launch (kernel-parameter space)
     const BoxDesc* boxes;
     int32_t nboxes;
-    uint32_t boxes_tile_cells;    // cells per tile (the same for every box of a launch)
+    uint32_t boxes_tile_cells;    // the largest tile (cells) of any box of the launch
+    const TileEntry* tile_info;   // ensembles: one entry per tile
     uint32_t num_tiles;
     uint64_t total_slots;
     uint64_t step;                // k: this launch completes step k (step_base: k - *step_base)

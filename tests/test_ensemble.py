@@ -3,7 +3,8 @@ by one launch per step.  Every draw is keyed by (box seed, step, box-local cell 
 particle), SRD cell sums are exact and the extended collision walks cells in
 particle-id order, so each box of an ensemble must evolve bit-identically to a
 single-box handle made from the same parameters -- including after the
-autotuner has changed the tiling.
+autotuner has changed the tiling.  Boxes of different density take tiles of
+different size within one launch (here 32 to 128 cells).
 """
 from __future__ import annotations
 
@@ -20,6 +21,7 @@ BOXES = [
     dict(L=(8, 16, 20), periodic=(1, 1, 0), n=20, drag=1e-2, seed=13),
     dict(L=(6, 5, 7), periodic=(1, 1, 1), n=8, drag=0.0, seed=14),
     dict(L=(32, 8, 40), periodic=(1, 1, 0), n=5, drag=3e-3, dt=0.05, temperature=0.5, seed=15),
+    dict(L=(8, 8, 12), periodic=(1, 1, 0), n=40, drag=2e-3, seed=16),
 ]
 
 
