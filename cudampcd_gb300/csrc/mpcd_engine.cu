@@ -154,20 +154,22 @@ public:
         check_device_errors();
     }
 
+    // Mean fields of the FP64 sums (kept in storage order), gathered into the
+    // reference order on the device: 16 bytes per cell cross to the host.
     void sample_mean(float* density, float* velocity)
     {
-        std::vector<SampleAcc> acc(cells_);
-        check(cudaMemcpyAsync(acc.data(), acc_.p, sizeof(SampleAcc) * cells_, cudaMemcpyDeviceToHost, stream_),
-              "sample read");
-        check(cudaStreamSynchronize(stream_), "sample read");
+        if (!mean_.p) check(mean_.alloc(sizeof(float) * 4 * cells_), "alloc mean fields");
+        float* d_density = mean_.as<float>();
+        float* d_velocity = d_density + cells_;
         // cpu_backend.cpp:218 / cuda_backend_impl.cu:210: divide by the counter, S-1 for S samples
         const double inverse = 1.0 / (double)sample_counter_;
-        for (uint64_t c = 0; c < cells_; ++c) {   // lab cells of every box, each in reference order
-            density[c] = (float)(acc[c].n * inverse);
-            velocity[3 * c + 0] = (float)(acc[c].vx * inverse);
-            velocity[3 * c + 1] = (float)(acc[c].vy * inverse);
-            velocity[3 * c + 2] = (float)(acc[c].vz * inverse);
-        }
+        for (const BoxDesc& b : boxes_)   // lab cells of every box, each in reference order
+            check(launch_mean_fields(acc_.as<SampleAcc>(), b, inverse, d_density, d_velocity, stream_), "mean fields");
+        check(cudaMemcpyAsync(density, d_density, sizeof(float) * cells_, cudaMemcpyDeviceToHost, stream_),
+              "sample read");
+        check(cudaMemcpyAsync(velocity, d_velocity, sizeof(float) * 3 * cells_, cudaMemcpyDeviceToHost, stream_),
+              "sample read");
+        check(cudaStreamSynchronize(stream_), "sample read");
         sampling_ = false;
     }
 
@@ -1250,6 +1252,7 @@ private:
     uint64_t step_ = 0;
     bool sampling_ = false;
     uint64_t sample_counter_ = 0;
+    DeviceBuffer mean_;   // mean fields of a read (4 floats per cell)
     bool use_table_ = false;
     bool last_step_table_ = false;
     bool dense_valid_ = false;   // dense_pos_ / dense_vel_ hold the state after step step_ - 1

@@ -14,6 +14,7 @@
 // (extended_collision_strategy.cu:17-332), the counting sort (sort_particles.cu)
 // and the sampling kernels (simulation_kernels.cu:150-230); the arithmetic
 // follows the CPU backend (cpu_backend/simulation_functions.cpp:38-406).
+#include <algorithm>
 #include <cstdio>
 #include <mutex>
 
@@ -445,14 +446,14 @@ __device__ void overflow_pass(const StepArgs& a, uint64_t step)
                 if (a.tape_key) {
                     const bool bounced = vs.x != v.x || vs.y != v.y || vs.z != v.z;
                     a.tape_key[id] = kTapeNone;
-                    a.tape_lab[id] = (b.cell_base + ref_index(b, cell_of_wrapped(b, x))) | (bounced ? kTapeBounce : 0u);
+                    a.tape_lab[id] = (b.cell_base + storage_index(b, cell_of_wrapped(b, x))) | (bounced ? kTapeBounce : 0u);
                 }
             }
         }
         if (a.replay) continue;
         const BoxDesc& b = a.boxes[bi];
         if (a.sample) {
-            const uint32_t lab = active ? b.cell_base + ref_index(b, cell_of_wrapped(b, x)) : 0;
+            const uint32_t lab = active ? b.cell_base + storage_index(b, cell_of_wrapped(b, x)) : 0;
             sample_add(a.samp, lab, v, active);
         }
         store_particle(a, b, xs, vs, id, key, active);
@@ -544,6 +545,7 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
         // ghost counts (its readers all passed the previous tile's last barrier)
         uint4 next_entry = make_uint4(0u, 0u, 0u, 0u);
         if (tid == kLocator) next_entry = tile_entry<SINGLE>(a, tile + gridDim.x);
+
         const float3 s = sshift[0];
         const float3 sn = sshift[1];
         const float shift_abs = fabsf(s.z);
@@ -801,7 +803,7 @@ __global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const
                 s_pos[p] = make_float4(xn.x, xn.y, xn.z, __uint_as_float(next));
                 s_vel[p] = make_float4(vn.x, vn.y, vn.z, vp.w);
                 const bool need_lab = a.sample || (ALGO == 0 && a.tape_key);
-                const uint32_t lab = need_lab ? b.cell_base + ref_index(b, cell_of_wrapped(b, x)) : 0u;
+                const uint32_t lab = need_lab ? b.cell_base + storage_index(b, cell_of_wrapped(b, x)) : 0u;
                 if (ALGO == 0 && a.tape_key) {
                     const uint32_t id = __float_as_uint(vp.w);
                     const bool bounced = vn.x != v.x || vn.y != v.y || vn.z != v.z;
@@ -1111,6 +1113,7 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(StepArgs a, const flo
 
 // Per lab cell: mean velocity of the step (0 for an empty cell, as averageReduceOnly)
 // into the FP64 running sums; snapshot or accumulate (cpu_backend.cpp:189-211).
+// Any cell order (the sums are kept in storage order).
 __global__ void sample_finalize_kernel(float4* samp, SampleAcc* acc, uint64_t cells, int snapshot,
                                        uint32_t* lab_count)
 {
@@ -1130,6 +1133,23 @@ __global__ void sample_finalize_kernel(float4* samp, SampleAcc* acc, uint64_t ce
         r.vz += (double)mz;
         acc[c] = r;
         samp[c] = make_float4(0, 0, 0, 0);
+    }
+}
+
+// Mean fields of one box in reference order (x fastest) from the FP64 sums, which
+// are kept in storage order: density n / S and velocity v / S per lab cell
+// (cpu_backend.cpp:218, `inverse` = 1 / S).
+__global__ void mean_fields_kernel(const SampleAcc* acc, BoxDesc b, double inverse, float* density, float* velocity)
+{
+    const uint32_t Lx = (uint32_t)b.L[0], Ly = (uint32_t)b.L[1], Lz = (uint32_t)b.L[2];
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < b.C; r += gridDim.x * blockDim.x) {
+        const uint32_t x = r % Lx, yz = r / Lx, y = yz % Ly, z = yz / Ly;
+        const SampleAcc q = acc[b.cell_base + z + Lz * (x + Lx * y)];
+        const uint64_t g = b.cell_base + (uint64_t)r;
+        density[g] = (float)(q.n * inverse);
+        velocity[3 * g + 0] = (float)(q.vx * inverse);
+        velocity[3 * g + 1] = (float)(q.vy * inverse);
+        velocity[3 * g + 2] = (float)(q.vz * inverse);
     }
 }
 
@@ -1351,14 +1371,15 @@ __global__ void subtract_kernel(float* vel, uint64_t begin, uint64_t end, float 
 //   lambda_{t,i} = R_c^T (mu_i - s_c) + s_c,  s_c = sum_{j in c} mu_j / N_c  (collided i; else mu_i),
 //   dL/dg += dt sum_{collided i} mu_{t,i,x},  and finally dL/dV0 = B_0 lambda_0.
 
-// U(z) of one box from the FP64 sample sums: one block per z layer.
+// U(z) of one box from the FP64 sample sums (storage order): one block per z layer.
 __global__ void __launch_bounds__(kThreads) profile_kernel(const SampleAcc* acc, BoxDesc b, double inv,
                                                            float* profile)
 {
     __shared__ double red[kThreads];
     const uint32_t per = (uint32_t)(b.L[0] * b.L[1]);
     double s = 0;
-    for (uint32_t k = threadIdx.x; k < per; k += kThreads) s += acc[b.cell_base + blockIdx.x * per + k].vx;
+    // layer z of the storage order: cells z + Lz k, k = x + Lx y
+    for (uint32_t k = threadIdx.x; k < per; k += kThreads) s += acc[b.cell_base + blockIdx.x + (uint64_t)b.L[2] * k].vx;
     red[threadIdx.x] = s;
     __syncthreads();
     for (int o = kThreads / 2; o > 0; o >>= 1) {
@@ -1376,13 +1397,13 @@ __global__ void __launch_bounds__(kThreads) adjoint_pass1_kernel(BoxDesc b, uint
 {
     __shared__ double red[kThreads];
     double gl = 0;
-    const uint32_t per = (uint32_t)(b.L[0] * b.L[1]);
+    const uint32_t Lz = (uint32_t)b.L[2];
     for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
         float3 m = make_float3(lam[3 * i], lam[3 * i + 1], lam[3 * i + 2]);
         const uint32_t l = lab[i];
         if (l & kTapeBounce) m = make_float3(-m.x, -m.y, -m.z);
         const uint32_t c = l & ~kTapeBounce;
-        const uint32_t z = (c - b.cell_base) / per;
+        const uint32_t z = (c - b.cell_base) % Lz;   // lab cells in storage order (z fastest)
         m.x += (float)((double)dU[z] * w / (double)lab_count[c]);
         lam[3 * i] = m.x; lam[3 * i + 1] = m.y; lam[3 * i + 2] = m.z;
         const uint32_t k = key[i];
@@ -1544,6 +1565,14 @@ cudaError_t launch_sample_finalize(float4* samp, SampleAcc* acc, uint64_t cells,
                                    cudaStream_t st, uint32_t* lab_count)
 {
     sample_finalize_kernel<<<grid, kThreads, 0, st>>>(samp, acc, cells, snapshot, lab_count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mean_fields(const SampleAcc* acc, const BoxDesc& b, double inverse, float* density, float* velocity,
+                               cudaStream_t st)
+{
+    const unsigned grid = (unsigned)std::min<uint64_t>((b.C + kThreads - 1) / kThreads, 4096);
+    mean_fields_kernel<<<grid, kThreads, 0, st>>>(acc, b, inverse, density, velocity);
     return cudaGetLastError();
 }
 

@@ -24,6 +24,10 @@ cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel
 // Lab-grid sample of one step into the FP64 running sums (and clear the step sums).
 cudaError_t launch_sample_finalize(float4* samp, SampleAcc* acc, uint64_t cells, int snapshot, int grid,
                                    cudaStream_t st, uint32_t* lab_count = nullptr);
+// Density and velocity means of one box in reference order (x fastest) from the
+// FP64 sums (storage order), divided by the sample count: inverse = 1 / samples.
+cudaError_t launch_mean_fields(const SampleAcc* acc, const BoxDesc& b, double inverse, float* density, float* velocity,
+                               cudaStream_t st);
 // Adjoint of the sampled x-velocity profile (single box, SRD): U(z) from the sample
 // sums of `samples` steps; one reverse step (both passes) at absolute step `step`;
 // dL/dV0 from the final adjoint and the bounce bits of the initial streaming.

@@ -126,7 +126,7 @@ struct StepArgs {
     float* dense_vel;
     DeviceState* state;
     int32_t sample;               // accumulate the lab-grid sample of clean(k+1)
-    float4* samp;                 // [global cells] (sum vx, vy, vz, count)
+    float4* samp;                 // [global lab cells, storage order] (sum vx, vy, vz, count)
     float ext_axis[13][3];        // discrete axis set of the extended collision
     DrawTables draws;             // used by the injected-draw instantiation
     // adjoint tape of this step, by particle id / cell (null: not recorded):

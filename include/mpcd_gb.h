@@ -178,9 +178,11 @@ int32_t mpcd_gb_ensemble_create(const mpcd_gb_params *params, int32_t R, mpcd_gb
 int32_t mpcd_gb_num_boxes(const mpcd_gb_handle *h);
 /* out = {first_particle, num_particles, first_cell, num_cells} of box r. */
 int32_t mpcd_gb_box_range(mpcd_gb_handle *h, int32_t r, uint64_t out[4]);
-/* Choose the tile size (cells per tile, a power of two in 8..128) and the particle
- * buffer of the step kernel by timing steps_per_candidate real steps of every
- * admissible pair (the steps advance the simulation); out = {tile cells, buffer}. */
+/* Choose the particle buffer of the step kernel and the tiles of every box (per box
+ * the largest power of two, 8..128 cells, whose expected particles times a fill
+ * factor fit the buffer) by timing steps_per_candidate real steps of every
+ * admissible (buffer, fill factor) pair; the steps advance the simulation.
+ * out = {largest tile of any box (cells), buffer (particles)}. */
 int32_t mpcd_gb_autotune(mpcd_gb_handle *h, int32_t steps_per_candidate, uint32_t out[2]);
 
 /* ---- device-pointer I/O and the differentiable channel (no counterpart in the reference) ---- */
@@ -226,9 +228,9 @@ int32_t mpcd_gb_profile_backward(mpcd_gb_handle *h, const float *d_grad_profile,
                                  double *grad_drag);
 /* Test hook: the fixed events of every step of the last profile forward, host arrays:
  * key[steps*N] (collision cell, storage order, or 0xFFFFFFFF if not collided),
- * lab[steps*N] (lab cell, reference order, | 0x80000000 if the streaming after that
+ * lab[steps*N] (lab cell, storage order, | 0x80000000 if the streaming after that
  * step bounced the particle), ncell[steps*C] (particles + ghosts of each collided cell,
- * storage order), lab_count[steps*C], bounce0[N] (0x80000000 if the streaming into the
+ * storage order), lab_count[steps*C] (storage order), bounce0[N] (0x80000000 if the streaming into the
  * first step bounced the particle).  Any pointer may be NULL. */
 int32_t mpcd_gb_profile_tape(mpcd_gb_handle *h, uint32_t *key, uint32_t *lab, uint32_t *ncell, uint32_t *lab_count,
                              uint32_t *bounce0);

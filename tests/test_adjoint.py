@@ -95,7 +95,7 @@ def fp64_profile(tape, L, seed, s0, dt, V0, g):
         Q[idx, 0] = Q[idx, 0] + g * dt
         labc = lab[t] & ~np.uint32(BOUNCE)
         w_lab = torch.from_numpy(1.0 / cnt[t][labc].astype(np.float64))
-        U = U.index_add(0, torch.from_numpy((labc // (Lx * Ly)).astype(np.int64)), Q[:, 0] * w_lab)
+        U = U.index_add(0, torch.from_numpy((labc % Lz).astype(np.int64)), Q[:, 0] * w_lab)   # storage order
         P = torch.where(torch.from_numpy(lab[t] & BOUNCE != 0)[:, None], -Q, Q)
     return U / (S * Lx * Ly)
 
