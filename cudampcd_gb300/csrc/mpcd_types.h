@@ -132,7 +132,7 @@ struct StepArgs {
     // adjoint tape of this step, by particle id / cell (null: not recorded):
     //   tape_key[id]  = collision cell (global storage index) if the particle was
     //                   collided (cell with n > 1), else kTapeNone;
-    //   tape_lab[id]  = lab cell it was sampled in (global, reference order) |
+    //   tape_lab[id]  = lab cell it was sampled in (global storage index) |
     //                   kTapeBounce if the streaming that follows bounced it;
     //   tape_ncell[c] = particles incl. ghosts of collided cell c (storage index).
     // The scatter records only the bounce bit of its streaming in tape_lab.
