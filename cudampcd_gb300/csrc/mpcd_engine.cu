@@ -704,7 +704,8 @@ public:
         double best_fill = fill_;
         uint32_t best_pbuf = pbuf_;
         std::vector<std::vector<uint32_t>> tried;   // tilings already timed (per-box tile cells + buffer)
-        for (uint32_t pbuf : {1024u, 1536u, 2048u}) {
+        // buffers: 1408 keeps 4 SRD CTAs per SM with 128-cell tiles, 1536 with 64
+        for (uint32_t pbuf : {1024u, 1280u, 1408u, 1536u, 2048u}) {
             if (pbuf < 5 * n_max) continue;
             for (double fill : {1.0, 1.15, 1.3, 1.6, 2.0, 3.0}) {
                 std::vector<uint32_t> key{pbuf};
@@ -828,9 +829,12 @@ private:
         if (total_slots_ + ov_cap_ >= (1ull << 32))
             throw Error(MPCD_GB_EINVAL, "cells * 4n exceeds the 32-bit slot space of one handle");
         // tiles: per box a power-of-two number of cells (a group of 256 / cells
-        // threads per cell) holding about pbuf / 1.15 particles; the buffer holds
-        // one cell with all its ghosts (cap + n = 5n) at least
-        uint32_t pbuf = std::max(1536u, 5 * n_max);
+        // threads per cell) holding up to pbuf particles on average; the buffer
+        // holds one cell with all its ghosts (cap + n = 5n) at least.  1408
+        // particles keep 4 SRD CTAs per SM even with 128-cell tiles (58 KB of
+        // shared memory at 1536 allows only 3); the autotuner confirmed it as the
+        // fastest buffer for n = 5, 10 and 20.
+        uint32_t pbuf = 5 * n_max <= 1408 ? 1408u : std::max(1536u, 5 * n_max);
         if (pbuf > 2048) throw Error(MPCD_GB_EINVAL, "n above 409: one cell and its ghosts must fit a tile");
         // tuning overrides (used by the tuning sweeps)
         if (const char* e = std::getenv("MPCD_GB_PBUF")) {
@@ -841,7 +845,7 @@ private:
             const uint32_t v = (uint32_t)std::strtoul(e, nullptr, 10);
             if (v >= 8 && v <= tile_cells_max() && (v & (v - 1)) == 0) forced_tile_cells_ = v;
         }
-        set_tiles(1.15, pbuf);
+        set_tiles(1.0, pbuf);
         float table[13][3];
         const int steps = 4;
         for (int select = 0; select <= 12; ++select) {   // simulation_functions.cpp:272-290
@@ -1247,7 +1251,7 @@ private:
     uint64_t N_ = 0, cells_ = 0, tiles_ = 0, total_slots_ = 0;
     uint32_t ov_cap_ = 0, pbuf_ = 0;
     uint32_t max_tile_cells_ = 0, forced_tile_cells_ = 0;   // largest tile of any box; a tile size forced for all
-    double fill_ = 1.15;                                     // expected particles per tile = pbuf / fill
+    double fill_ = 1.0;                                      // expected particles per tile = pbuf / fill
     float ext_axis_[13][3];
     uint64_t step_ = 0;
     bool sampling_ = false;
