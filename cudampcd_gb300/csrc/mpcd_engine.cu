@@ -704,8 +704,8 @@ public:
         double best_fill = fill_;
         uint32_t best_pbuf = pbuf_;
         std::vector<std::vector<uint32_t>> tried;   // tilings already timed (per-box tile cells + buffer)
-        // buffers: 1408 keeps 4 SRD CTAs per SM with 128-cell tiles, 1536 with 64
-        for (uint32_t pbuf : {1024u, 1280u, 1408u, 1536u, 2048u}) {
+        // buffers: 1408 keeps 4 SRD CTAs per SM with 128-cell tiles, 1344 extended ones
+        for (uint32_t pbuf : {1024u, 1280u, 1344u, 1408u, 1536u, 2048u}) {
             if (pbuf < 5 * n_max) continue;
             for (double fill : {1.0, 1.15, 1.3, 1.6, 2.0, 3.0}) {
                 std::vector<uint32_t> key{pbuf};
@@ -830,11 +830,13 @@ private:
             throw Error(MPCD_GB_EINVAL, "cells * 4n exceeds the 32-bit slot space of one handle");
         // tiles: per box a power-of-two number of cells (a group of 256 / cells
         // threads per cell) holding up to pbuf particles on average; the buffer
-        // holds one cell with all its ghosts (cap + n = 5n) at least.  1408
-        // particles keep 4 SRD CTAs per SM even with 128-cell tiles (58 KB of
-        // shared memory at 1536 allows only 3); the autotuner confirmed it as the
-        // fastest buffer for n = 5, 10 and 20.
-        uint32_t pbuf = 5 * n_max <= 1408 ? 1408u : std::max(1536u, 5 * n_max);
+        // holds one cell with all its ghosts (cap + n = 5n) at least.  The
+        // default buffer keeps 4 CTAs per SM: 1408 particles with SRD's 128-cell
+        // tiles (at 1536 their 58 KB of shared memory allows only 3), 1344 with the
+        // extended collision's 64-cell tiles (38 B per particle); the autotuner
+        // confirmed both as the fastest buffers at n = 5, 10 and 20.
+        const uint32_t pbuf_default = params_.algorithm == 1 ? 1344u : 1408u;
+        uint32_t pbuf = 5 * n_max <= pbuf_default ? pbuf_default : std::max(1536u, 5 * n_max);
         if (pbuf > 2048) throw Error(MPCD_GB_EINVAL, "n above 409: one cell and its ghosts must fit a tile");
         // tuning overrides (used by the tuning sweeps)
         if (const char* e = std::getenv("MPCD_GB_PBUF")) {

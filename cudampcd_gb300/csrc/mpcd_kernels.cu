@@ -473,10 +473,11 @@ __device__ __forceinline__ T group_sum(T v, uint32_t G)
     return v;
 }
 
-// SRD: 4 CTAs of 256 threads per SM (64 registers, about 54 KB of shared memory each);
-// extended: 3 (its tile carries two more arrays)
+// 4 CTAs of 256 threads per SM: 64 registers, and at most about 56 KB of shared
+// memory each (SRD: a 1408-particle buffer with 128-cell tiles; extended, whose
+// tile carries two more arrays: 1344 particles with 64-cell tiles)
 template <int ALGO, bool TABLE, bool SINGLE, bool REPLAY>
-__global__ void __launch_bounds__(kThreads, ALGO == 0 ? 4 : 3) step_kernel(const StepArgs a, uint32_t pbuf)
+__global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uint32_t pbuf)
 {
     using D = Draws<TABLE>;
     extern __shared__ __align__(128) unsigned char dyn[];
