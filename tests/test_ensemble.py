@@ -77,6 +77,29 @@ def test_boxes_evolve_as_single_handles(alg):
             h.close()
 
 
+@pytest.mark.parametrize("alg", [0, 1])
+def test_dense_boxes_take_small_tiles_and_sub_tiles(alg):
+    """Densities from 5 to 200 in one launch: 128- or 64-cell tiles down to 8-cell
+    tiles with one warp per cell, and at n = 200 tiles whose particles exceed the
+    buffer and run as several sub-tiles -- each box still as its single handle."""
+    boxes = [dict(L=(10, 8, 14), periodic=(1, 1, 0), n=5, drag=1e-3, seed=21, algorithm=alg),
+             dict(L=(6, 6, 12), periodic=(1, 1, 0), n=100, drag=2e-3, seed=22, algorithm=alg),
+             dict(L=(5, 6, 10), periodic=(1, 1, 1), n=200, drag=0.0, seed=23, algorithm=alg),
+             dict(L=(8, 8, 12), periodic=(1, 1, 0), n=20, drag=1e-3, seed=24, algorithm=alg)]
+    ens = capi.Handle(boxes=boxes)
+    singles = [capi.Handle(**b) for b in boxes]
+    try:
+        ens.step(5)
+        for h in singles:
+            h.step(5)
+        _check_same(ens, singles)
+        assert ens.counters() == (0, 0)
+    finally:
+        ens.close()
+        for h in singles:
+            h.close()
+
+
 def test_ensemble_rejects_mixed_algorithms_and_empty():
     with pytest.raises(capi.GbError, match="same algorithm"):
         capi.Handle(boxes=[dict(BOXES[0], algorithm=0), dict(BOXES[1], algorithm=1)])
