@@ -229,6 +229,9 @@ EXTREME = {
     # dense cells: 16-cell tiles, up to 5n = 320 staged entries in one cell with its ghosts
     "srd_dense": O.Box(L=(4, 4, 6), periodic=(1, 1, 0), algorithm=O.SRD, n=64, dt=0.02, drag=0.001),
     "ext_dense": O.Box(L=(4, 3, 5), periodic=(1, 1, 0), algorithm=O.EXTENDED, n=64, dt=0.02, drag=0.001),
+    # the densest accepted n: the particle buffer is 5n = 2045 entries (a full
+    # bucket and its ghosts), and 8-cell tiles run as several sub-tiles
+    "srd_max_density": O.Box(L=(3, 3, 4), periodic=(1, 1, 0), algorithm=O.SRD, n=409, dt=0.02, drag=0.001),
     # a single fluid layer between the walls
     "srd_one_layer": O.Box(L=(6, 6, 3), periodic=(1, 1, 0), algorithm=O.SRD, n=10, dt=0.05, drag=0.01),
 }
