@@ -21,7 +21,12 @@ g = 0.0005): warm-up, then the wall pressure, the density profile and the
 viscosity from the curvature of the sampled velocity profile.  --physics srd
 runs the same measurement with the SRD collision.  --eta-guess E starts the
 flow from the steady Poiseuille profile of viscosity E (the warm-up then only
-has to relax the guess's error).
+has to relax the guess's error).  --physics viscosity runs the SRD viscosity
+channel of the reference's own check (10 x 10 x 100 cells + 2 walls, n = 10,
+g = 0.001, dt = 0.02) as 16 replicas in one handle, with the reference's protocol
+(1000 warm-up steps, 100000 sampled) and with a warm-up of five relaxation times
+(67500 steps), each read with the reference's estimator (README.md:94-96:
+L^2 n g / (8 max u)) and with the curvature fit.
 
 Profiling options (the default run uses none of them): --size LX LY LZ replaces
 the fluid cells of the workload (walls are added in z), --algorithm extended
@@ -435,6 +440,45 @@ def run_physics(args):
     print(json.dumps(out), flush=True)
 
 
+def run_viscosity(args):
+    """SRD viscosity of the 10 x 10 x 100 channel, R replicas advanced as one
+    batched handle (per-replica Philox seeds 2024 + r): eta per replica from the
+    reference's estimator and from the curvature fit; mean and standard error
+    over the replicas.  Analytic value (1 - cos a) / (18 dt) (n - 1 + e^-n)."""
+    import numpy as np
+
+    from cudampcd_gb300 import capi
+
+    R, Lx, Ly, Lz, n, g, dt = 16, 10, 10, 100, 10, 0.001, 0.02
+    theory = (1 - np.cos(2 * np.pi / 3)) / (18 * dt) * (n - 1 + np.exp(-n))
+    zc = np.arange(Lz + 2) + 0.5 - (Lz + 2) / 2.0
+    fluid = slice(1, Lz + 1)
+    A = np.stack([np.ones(Lz), -(zc[fluid] ** 2 + 1.0 / 12.0)], axis=1)
+    out = {"physics": "viscosity", "workload": f"SRD channel {Lx}x{Ly}x{Lz} cells + 2 walls, n={n}, T=1, dt={dt}, "
+                                               f"g={g}, {R} replicas in one handle, seeds 2024+r",
+           "srd_theory": float(theory), "protocols": {}}
+    for name, warm, sampled in (("reference: 1000 warm-up, 100000 sampled", 1000, 100000),
+                                ("5 relaxation times warm-up, 100000 sampled", 67500, 100000)):
+        h = capi.Handle(boxes=[dict(L=(Lx, Ly, Lz + 2), periodic=(1, 1, 0), n=n, dt=dt, drag=g, seed=2024 + r)
+                               for r in range(R)])
+        t0 = time.perf_counter()
+        h.step(warm)
+        h.step_and_sample(sampled)
+        _, v = h.sample_mean()
+        elapsed = time.perf_counter() - t0
+        flags = h.counters()[1]
+        h.close()
+        u = v[:, 0].reshape(R, Lz + 2, Ly, Lx).mean(axis=(2, 3)).astype(np.float64)   # as get_mean_fields gives it
+        eta_max = Lz * Lz * n * g / (8.0 * u.max(axis=1))
+        eta_fit = np.array([n * g / (2.0 * np.linalg.lstsq(A, ur[fluid] * (sampled - 1) / sampled, rcond=None)[0][1])
+                            for ur in u])
+        out["protocols"][name] = {
+            "reference_estimator": {"mean": float(eta_max.mean()), "stderr": float(eta_max.std(ddof=1) / np.sqrt(R))},
+            "curvature_fit": {"mean": float(eta_fit.mean()), "stderr": float(eta_fit.std(ddof=1) / np.sqrt(R))},
+            "seconds": elapsed, "error_flags": flags}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -448,7 +492,7 @@ def main():
     ap.add_argument("--algorithm", default="srd", choices=["srd", "extended"])
     ap.add_argument("--ensemble", type=int, default=0, metavar="R")
     ap.add_argument("--small-replicas", dest="small_replicas", action="store_true")
-    ap.add_argument("--physics", choices=["extended", "srd"])
+    ap.add_argument("--physics", choices=["extended", "srd", "viscosity"])
     ap.add_argument("--eta-guess", dest="eta_guess", type=float, default=0.0)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -458,6 +502,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
     if args.ensemble:
         run_ensemble(args)
+    elif args.physics == "viscosity":
+        run_viscosity(args)
     elif args.physics:
         run_physics(args)
     elif args.impl == "reference":
