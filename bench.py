@@ -310,7 +310,7 @@ def run_gpu_arm(args, rank, world, local_rank):
                          "kernel": f"step_kernel<{args.algorithm.upper()}, Philox>", "kernel_ms": per_launch_ms},
             "e2e": e2e,
             "clocks": clocks.summary(),
-            "gpu_launches": args.steps,
+            "gpu_launches": 2 * args.steps,   # per step: overflow selection, step kernel
             "device_counters": {"bucket_overflows": overflowed, "error_flags": flags},
         }
         if not args.no_cpu:

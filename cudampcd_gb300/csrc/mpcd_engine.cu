@@ -652,11 +652,7 @@ public:
         std::vector<cudaEvent_t> ks(2 * (size_t)n);
         for (auto& e : ks) check(cudaEventCreate(&e), "event");
         check(cudaEventRecord(e0, stream_), "event");
-        for (int i = 0; i < n; ++i) {
-            check(cudaEventRecord(ks[2 * i], stream_), "event");
-            launch_one_step(false);
-            check(cudaEventRecord(ks[2 * i + 1], stream_), "event");
-        }
+        for (int i = 0; i < n; ++i) launch_one_step(false, ks[2 * i], ks[2 * i + 1]);
         check(cudaEventRecord(e1, stream_), "event");
         check(cudaEventSynchronize(e1), "event");
         float t = 0, k = 0;
@@ -930,6 +926,8 @@ private:
             check(vel_[k].alloc(sizeof(float4) * total_slots_), "alloc bucket velocities");
             check(ov_pos_[k].alloc(sizeof(float4) * ov_cap_), "alloc overflow list");
             check(ov_vel_[k].alloc(sizeof(float4) * ov_cap_), "alloc overflow list");
+            check(ov_next_[k].alloc(sizeof(uint32_t) * ov_cap_), "alloc overflow chains");
+            check(ov_head_[k].alloc(sizeof(uint32_t) * cells_), "alloc overflow chains");
         }
         for (int k = 0; k < 3; ++k) {
             check(count_[k].alloc(sizeof(uint32_t) * cells_), "alloc counts");
@@ -1018,6 +1016,10 @@ private:
         a.ov_in_slot = (uint32_t)(k % 3);
         a.ov_out_slot = (uint32_t)((k + 1) % 3);
         a.ov_zero_slot = (uint32_t)((k + 2) % 3);
+        a.ov_head_in = ov_head_[p].as<uint32_t>();
+        a.ov_head_out = ov_head_[q].as<uint32_t>();
+        a.ov_next_in = ov_next_[p].as<uint32_t>();
+        a.ov_next_out = ov_next_[q].as<uint32_t>();
         a.state = state_.as<DeviceState>();
         a.samp = samp_.as<float4>();
         std::memcpy(a.ext_axis, ext_axis_, sizeof ext_axis_);
@@ -1065,7 +1067,8 @@ private:
             StepArgs a = args((uint64_t)i);   // buffers of step i == those of any step = i mod 6
             a.step_base = step_base_ptr();
             a.sample = sample ? 1 : 0;
-            err = launch_step(a, params_.algorithm, false, pbuf_, grid_, cs);
+            err = select_overflow(a, (uint64_t)i, cs);
+            if (err == cudaSuccess) err = launch_step(a, params_.algorithm, false, pbuf_, grid_, cs);
             if (err == cudaSuccess && sample)
                 err = launch_sample_finalize(samp_.as<float4>(), acc_.as<SampleAcc>(), cells_, 0, sms_ * 8, cs);
         }
@@ -1097,11 +1100,25 @@ private:
         return done;
     }
 
-    void launch_one_step(bool sample)
+    // The reference's choice of the particles that collide in overflowing cells,
+    // made on the inputs of step k before its kernel runs.
+    cudaError_t select_overflow(const StepArgs& a, uint64_t k, cudaStream_t st)
+    {
+        const unsigned p = (unsigned)(k & 1);
+        return launch_overflow_select(a, pos_[p].as<float4>(), vel_[p].as<float4>(), ov_pos_[p].as<float4>(),
+                                      ov_vel_[p].as<float4>(), sms_, st);
+    }
+
+    // One step: the overflow selection, then the step kernel (bracketed by the
+    // events `before` and `after` when given, which time the step kernel alone).
+    void launch_one_step(bool sample, cudaEvent_t before = nullptr, cudaEvent_t after = nullptr)
     {
         StepArgs a = args(step_);
         a.sample = sample ? 1 : 0;
+        check(select_overflow(a, step_, stream_), "overflow selection");
+        if (before) check(cudaEventRecord(before, stream_), "event");
         check(launch_step(a, params_.algorithm, use_table_, pbuf_, grid_, stream_), "step kernel");
+        if (after) check(cudaEventRecord(after, stream_), "event");
         last_step_table_ = use_table_;   // a replay of this step must consume the same draws
         use_table_ = false;
         ++step_;
@@ -1156,6 +1173,7 @@ private:
             a.tape_key = tkey_.as<uint32_t>() + (size_t)i * N_;
             a.tape_lab = tlab_.as<uint32_t>() + (size_t)i * N_;
             a.tape_ncell = tncell_.as<uint32_t>() + (size_t)i * cells_;
+            check(select_overflow(a, step_, stream_), "overflow selection");
             check(launch_step(a, params_.algorithm, false, pbuf_, grid_, stream_), "tape step");
             check(launch_sample_finalize(samp_.as<float4>(), acc_.as<SampleAcc>(), cells_, 1, sms_ * 8, stream_,
                                          tcnt_.as<uint32_t>() + (size_t)i * cells_),
@@ -1268,6 +1286,7 @@ private:
     float inject_shift_[kMaxInjectedShifts][3] = {};
     std::vector<TileEntry> tile_info_;   // tile table of the current tiling
     DeviceBuffer tile_info_d_;
+    DeviceBuffer ov_head_[2], ov_next_[2];   // overflow chains: heads by cell, links by entry (by step parity)
     DeviceBuffer boxes_d_, pos_[2], vel_[2], count_[3], ov_pos_[2], ov_vel_[2], state_, samp_, acc_, dense_pos_,
         dense_vel_, offsets_, scan_status_, scan_counter_, partial_;
     DeviceBuffer t_count_, t_gpos_, t_gvel_, t_axis_, t_gate_, t_gauss_;

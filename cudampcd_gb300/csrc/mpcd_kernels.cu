@@ -172,6 +172,21 @@ __device__ __forceinline__ void sample_add(float4* samp, uint32_t lab, float3 v,
     if (active) atomicAdd(samp + lab, make_float4(v.x, v.y, v.z, 1.0f));
 }
 
+// A particle that found the bucket of cell `key` full: into the overflow list of
+// the next step, chained to its cell (overflow_select_kernel walks the chain).
+__device__ __forceinline__ void push_overflow(const StepArgs& a, uint32_t key, float4 xp, float4 vp)
+{
+    atomicAdd(&a.state->overflow_total, 1ull);
+    const unsigned q = atomicAdd(&a.state->ov_count[a.ov_out_slot], 1u);
+    if (q < a.ov_cap) {
+        a.ov_out_pos[q] = xp;
+        a.ov_out_vel[q] = vp;
+        a.ov_next_out[q] = atomicExch(a.ov_head_out + key, q);
+    } else {
+        atomicOr(&a.state->error_flags, kErrOverflowListFull);
+    }
+}
+
 // Put one particle (already streamed and shifted for the next collision, in
 // cell `key`) into its bucket, or into the overflow list when the bucket is full.
 __device__ __forceinline__ void store_particle(const StepArgs& a, const BoxDesc& b, float3 xs, float3 vs, uint32_t id,
@@ -185,14 +200,7 @@ __device__ __forceinline__ void store_particle(const StepArgs& a, const BoxDesc&
         a.out_pos[at] = xp;
         a.out_vel[at] = vp;
     } else {
-        atomicAdd(&a.state->overflow_total, 1ull);
-        const unsigned q = atomicAdd(&a.state->ov_count[a.ov_out_slot], 1u);
-        if (q < a.ov_cap) {
-            a.ov_out_pos[q] = xp;
-            a.ov_out_vel[q] = vp;
-        } else {
-            atomicOr(&a.state->error_flags, kErrOverflowListFull);
-        }
+        push_overflow(a, key, xp, vp);
     }
 }
 
@@ -1051,14 +1059,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                         a.out_pos[at] = xp;
                         a.out_vel[at] = vp;
                     } else {
-                        atomicAdd(&a.state->overflow_total, 1ull);
-                        const unsigned q = atomicAdd(&a.state->ov_count[a.ov_out_slot], 1u);
-                        if (q < a.ov_cap) {
-                            a.ov_out_pos[q] = xp;
-                            a.ov_out_vel[q] = vp;
-                        } else {
-                            atomicOr(&a.state->error_flags, kErrOverflowListFull);
-                        }
+                        push_overflow(a, key[j], xp, vp);
                     }
                 }
             }
@@ -1072,6 +1073,51 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
             float v = imp[w];
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
             if (lane == 0 && v != 0.0f) atomicAdd(&a.state->wall_impulse[w], (double)v);
+        }
+    }
+}
+
+// Before step k: in every cell that received more particles than its bucket
+// holds (raw count > cap), keep the cap lowest ids in the bucket and move the
+// others to the overflow list, whatever order the claims of step k-1 arrived in:
+// the reference fills each cell's table in particle-index order, and the
+// particles past its depth skip the collision (simulation_functions.cpp:83-101).
+// The thread of a cell's last overflow entry (the head of the cell's chain) walks
+// the raw - cap entries of the chain; each in turn stays in the list or swaps
+// with the bucket's largest id.  Overflow is rare: without any, every thread
+// returns after one load.  Run on the inputs of step k, so a replay of step k
+// finds them already in order.
+__global__ void __launch_bounds__(kThreads) overflow_select_kernel(const StepArgs a, float4* in_pos, float4* in_vel,
+                                                                   float4* ov_pos, float4* ov_vel)
+{
+    const uint32_t n = min(a.state->ov_count[a.ov_in_slot], a.ov_cap);
+    for (uint32_t e0 = blockIdx.x * blockDim.x + threadIdx.x; e0 < n; e0 += gridDim.x * blockDim.x) {
+        const float4 p0 = ov_pos[e0];
+        const int bi = box_of_particle(a.boxes, a.nboxes, __float_as_uint(ov_vel[e0].w));
+        const BoxDesc& b = a.boxes[bi];
+        const uint32_t key = b.cell_base + storage_index(b, cell_of_wrapped(b, make_float3(p0.x, p0.y, p0.z)));
+        if (a.ov_head_in[key] != e0) continue;   // not the head of its cell's chain
+        const uint32_t raw = a.in_count[key];
+        const uint64_t base = b.slot_base + (uint64_t)(key - b.cell_base) * b.cap;
+        uint32_t e = e0;
+        for (uint32_t t = b.cap; t < raw && e < a.ov_cap; ++t) {
+            const uint32_t before = a.ov_next_in[e];
+            uint32_t jmax = 0, idmax = __float_as_uint(in_vel[base].w);
+            for (uint32_t j = 1; j < b.cap; ++j) {
+                const uint32_t id = __float_as_uint(in_vel[base + j].w);
+                if (id > idmax) {
+                    idmax = id;
+                    jmax = j;
+                }
+            }
+            const float4 pe = ov_pos[e], we = ov_vel[e];
+            if (__float_as_uint(we.w) < idmax) {
+                ov_pos[e] = in_pos[base + jmax];
+                ov_vel[e] = in_vel[base + jmax];
+                in_pos[base + jmax] = pe;
+                in_vel[base + jmax] = we;
+            }
+            e = before;
         }
     }
 }
@@ -1518,6 +1564,7 @@ cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* bl
     cudaFuncAttributes attr;
     e = cudaFuncGetAttributes(&attr, (const void*)advance_kernel);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, (const void*)sample_finalize_kernel);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, (const void*)overflow_select_kernel);
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         blocks_per_sm, (const void*)kStepFns[algorithm ? 1 : 0][0][1][0], kThreads, smem);
@@ -1559,6 +1606,13 @@ cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel
                            cudaStream_t st)
 {
     scatter_kernel<<<grid, kThreads, 0, st>>>(a, pos, vel, n_total);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_overflow_select(const StepArgs& a, float4* in_pos, float4* in_vel, float4* ov_pos, float4* ov_vel,
+                                   int grid, cudaStream_t st)
+{
+    overflow_select_kernel<<<grid, kThreads, 0, st>>>(a, in_pos, in_vel, ov_pos, ov_vel);
     return cudaGetLastError();
 }
 

@@ -21,6 +21,11 @@ cudaError_t launch_advance(DeviceState* state, unsigned steps, cudaStream_t st);
 // Key dense clean particles for step a.step + 1 and scatter them into a.out_*.
 cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel, uint64_t n_total, int grid,
                            cudaStream_t st);
+// Before a step (not a replay): the particles the reference keeps in each overflowing
+// cell into its bucket, the others into the overflow list (in_* / ov_*: the step's
+// input buckets and list, a.in_count, a.ov_head_in and a.ov_next_in its chains).
+cudaError_t launch_overflow_select(const StepArgs& a, float4* in_pos, float4* in_vel, float4* ov_pos, float4* ov_vel,
+                                   int grid, cudaStream_t st);
 // Lab-grid sample of one step into the FP64 running sums (and clear the step sums).
 cudaError_t launch_sample_finalize(float4* samp, SampleAcc* acc, uint64_t cells, int snapshot, int grid,
                                    cudaStream_t st, uint32_t* lab_count = nullptr);

@@ -119,6 +119,16 @@ struct StepArgs {
     float4* ov_out_vel;
     uint32_t ov_cap;
     uint32_t ov_in_slot, ov_out_slot, ov_zero_slot;   // indices into DeviceState::ov_count
+    // overflow chains: per cell the list entry of the last particle that found the
+    // cell's bucket full, per entry the one before it.  Heads alternate by step
+    // parity and are never cleared: a step reads the head of a cell only when the
+    // cell's count exceeds its depth, so the previous step's claims wrote it, and
+    // it follows exactly count - depth links (the last one would lead to older
+    // entries).
+    const uint32_t* ov_head_in;
+    uint32_t* ov_head_out;
+    const uint32_t* ov_next_in;   // by entry of ov_in
+    uint32_t* ov_next_out;        // by entry of ov_out
     // replay: recompute collision k and write the post-collision state to dense
     // (N, 3) arrays by particle id, changing nothing else
     int32_t replay;
