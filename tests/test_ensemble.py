@@ -100,6 +100,28 @@ def test_dense_boxes_take_small_tiles_and_sub_tiles(alg):
             h.close()
 
 
+@pytest.mark.parametrize("alg", [0, 1])
+def test_overflowing_boxes_evolve_as_single_handles(alg):
+    """At n = 1 and 2 some cells receive more particles than their buckets hold;
+    the lowest ids collide whatever order the claims arrived in, so an ensemble
+    still reproduces its single handles bit for bit."""
+    boxes = [dict(L=(12, 10, 12), periodic=(1, 1, 0), n=1, drag=1e-3, seed=31, algorithm=alg),
+             dict(L=(10, 12, 10), periodic=(1, 1, 1), n=2, drag=0.0, seed=32, algorithm=alg)]
+    ens = capi.Handle(boxes=boxes)
+    singles = [capi.Handle(**b) for b in boxes]
+    try:
+        ens.step(8)
+        for h in singles:
+            h.step(8)
+        _check_same(ens, singles)
+        overflowed, flags = ens.counters()
+        assert overflowed > 0 and flags == 0
+    finally:
+        ens.close()
+        for h in singles:
+            h.close()
+
+
 def test_ensemble_rejects_mixed_algorithms_and_empty():
     with pytest.raises(capi.GbError, match="same algorithm"):
         capi.Handle(boxes=[dict(BOXES[0], algorithm=0), dict(BOXES[1], algorithm=1)])
