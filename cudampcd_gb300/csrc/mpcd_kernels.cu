@@ -1081,7 +1081,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
 // holds (raw count > cap), keep the cap lowest ids in the bucket and move the
 // others to the overflow list, whatever order the claims of step k-1 arrived in:
 // the reference fills each cell's table in particle-index order, and the
-// particles past its depth skip the collision (simulation_functions.cpp:83-101).
+// particles past its depth skip the collision (simulation_functions.cpp:87-93).
 // The thread of a cell's last overflow entry (the head of the cell's chain) walks
 // the raw - cap entries of the chain; each in turn stays in the list or swaps
 // with the bucket's largest id.  Overflow is rare: without any, every thread
