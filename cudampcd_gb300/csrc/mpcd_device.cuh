@@ -107,6 +107,16 @@ __device__ __forceinline__ float3 pbc(const BoxDesc& b, float3 r)
     return pbc_general(b, r);
 }
 
+// pbc() of a position within half a cell of the box, such as x - s for a wrapped
+// x and a grid shift |s| <= 1/2: a = r + 1.5L then lies in [0, 3L) for any L >= 1,
+// so the range check is skipped; the arithmetic, and so the result, is pbc()'s.
+__device__ __forceinline__ float3 pbc_near(const BoxDesc& b, float3 r)
+{
+    return make_float3(pbc1_fast(r.x + b.L15[0], b.Lf[0], b.L2x[0]) - b.Lh[0],
+                       pbc1_fast(r.y + b.L15[1], b.Lf[1], b.L2x[1]) - b.Lh[1],
+                       pbc1_fast(r.z + b.L15[2], b.Lf[2], b.L2x[2]) - b.Lh[2]);
+}
+
 // Coordinate of a cell along one axis: floor(x + L/2) mod L, with the
 // float -> uint32 conversion of the reference's x86-64 build (via int64).
 __device__ __forceinline__ uint32_t cell_coord(float x, float Lf, float Lh, uint32_t L)

@@ -770,7 +770,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                         v = make_float3(__fmaf_rn(b.sin_a, cr.x, __fmaf_rn(b.cos_a, vperp.x, vpara.x)) + mean.x,
                                         __fmaf_rn(b.sin_a, cr.y, __fmaf_rn(b.cos_a, vperp.y, vpara.y)) + mean.y,
                                         __fmaf_rn(b.sin_a, cr.z, __fmaf_rn(b.cos_a, vperp.z, vpara.z)) + mean.z);
-                        x = pbc(b, make_float3(x.x - s.x, x.y - s.y, x.z - s.z));
+                        x = pbc_near(b, make_float3(x.x - s.x, x.y - s.y, x.z - s.z));   // staged x is wrapped
                         v.x += b.drag_dt;
                         collided = true;
                     }
