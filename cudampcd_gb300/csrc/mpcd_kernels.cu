@@ -784,7 +784,8 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                         v.x += b.drag_dt;
                         const float3 cr = cross3(x, omega);
                         v.x -= cr.x; v.y -= cr.y; v.z -= cr.z;
-                        x = pbc(b, make_float3((com.x + x.x) - s.x, (com.y + x.y) - s.y, (com.z + x.z) - s.z));
+                        // com + x rebuilds the wrapped staged position to within rounding
+                        x = pbc_near(b, make_float3((com.x + x.x) - s.x, (com.y + x.y) - s.y, (com.z + x.z) - s.z));
                         collided = true;
                     }
                 }
