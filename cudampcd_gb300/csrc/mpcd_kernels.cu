@@ -757,20 +757,19 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                 bool collided = false;
                 if (ALGO == 0) {
                     if (n > 1) {
-                        // v' = u + cos a vr + (1 - cos a)(vr . axis) axis + sin a (vr x axis),
-                        // vr = v - u: the reference's v_par + cos a v_perp + sin a (v_perp x
-                        // axis) rearranged (v_perp x axis = vr x axis), with fused
+                        // v' = u + v_par + cos a v_perp + sin a (v_perp x axis), with fused
                         // multiply-adds (the collision is compared to 1e-5, not bit-exactly)
                         const float3 axis = make_float3(k1.x, k1.y, k1.z);
                         const float3 vr = make_float3(v.x - mean.x, v.y - mean.y, v.z - mean.z);
                         const float vd = __fmaf_rn(vr.x, axis.x, __fmaf_rn(vr.y, axis.y, vr.z * axis.z));
-                        const float t = (1.0f - b.cos_a) * vd;
-                        const float3 cr = make_float3(__fmaf_rn(vr.y, axis.z, -(vr.z * axis.y)),
-                                                      __fmaf_rn(vr.z, axis.x, -(vr.x * axis.z)),
-                                                      __fmaf_rn(vr.x, axis.y, -(vr.y * axis.x)));
-                        v = make_float3(__fmaf_rn(t, axis.x, __fmaf_rn(b.cos_a, vr.x, __fmaf_rn(b.sin_a, cr.x, mean.x))),
-                                        __fmaf_rn(t, axis.y, __fmaf_rn(b.cos_a, vr.y, __fmaf_rn(b.sin_a, cr.y, mean.y))),
-                                        __fmaf_rn(t, axis.z, __fmaf_rn(b.cos_a, vr.z, __fmaf_rn(b.sin_a, cr.z, mean.z))));
+                        const float3 vpara = make_float3(axis.x * vd, axis.y * vd, axis.z * vd);
+                        const float3 vperp = make_float3(vr.x - vpara.x, vr.y - vpara.y, vr.z - vpara.z);
+                        const float3 cr = make_float3(__fmaf_rn(vperp.y, axis.z, -(vperp.z * axis.y)),
+                                                      __fmaf_rn(vperp.z, axis.x, -(vperp.x * axis.z)),
+                                                      __fmaf_rn(vperp.x, axis.y, -(vperp.y * axis.x)));
+                        v = make_float3(__fmaf_rn(b.sin_a, cr.x, __fmaf_rn(b.cos_a, vperp.x, vpara.x)) + mean.x,
+                                        __fmaf_rn(b.sin_a, cr.y, __fmaf_rn(b.cos_a, vperp.y, vpara.y)) + mean.y,
+                                        __fmaf_rn(b.sin_a, cr.z, __fmaf_rn(b.cos_a, vperp.z, vpara.z)) + mean.z);
                         x = pbc_near(b, make_float3(x.x - s.x, x.y - s.y, x.z - s.z));   // staged x is wrapped
                         v.x += b.drag_dt;
                         collided = true;
