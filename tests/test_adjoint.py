@@ -153,9 +153,9 @@ def test_adjoint_matches_central_differences_with_common_random_numbers():
     differences are exact up to FP32 rounding.  A small box and a short horizon
     keep event flips rare at perturbations FP32 still resolves.  The sampled
     profile sums velocities with float atomics, whose rounding varies from run to
-    run (about 3e-4 of the velocity difference quotient at the largest
+    run (by up to about 3e-4 of the velocity difference quotient at the largest
     event-preserving perturbation), so each loss is the mean of three runs and the
-    bound is 2e-3; the FP64 autograd test above pins the adjoint itself (to 1e-4,
+    bound is 2e-3 (measured 4e-4 to 7e-4); the FP64 autograd test above pins the adjoint itself (to 1e-4,
     measured 6e-7)."""
     L, n, drag0, dt, seed, S, K = (4, 4, 6), 10, 1e-3, 0.02, 9, 12, 4
     h = capi.Handle(L=L, periodic=(1, 1, 0), n=n, dt=dt, drag=drag0, seed=seed)
