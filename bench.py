@@ -32,12 +32,26 @@ Profiling options (the default run uses none of them): --size LX LY LZ replaces
 the fluid cells of the workload (walls are added in z), --algorithm extended
 switches the collision, --no-e2e and --no-cpu skip those parts.
 
+Adjoint: --adjoint times the differentiable channel (64 x 64 x 32 cells + 2 walls,
+n = 10, 200 steps, checkpoints every 20): a plain step, the sampled forward with
+checkpoints, and the adjoint (backward) per step, and their ratios.
+
 One JSON line on rank 0.  `value` is device-timed particle-steps/s with the
 state resident in HBM; `e2e` is the same metric through the Python API the
 reference exposes (Simulation.step_and_sample + get_mean_fields, host wall
-clock, results read back to the host).  `--impl reference` times the
-reference's CPU step (the oracle's restatement of it; the reference binary
-where it was built) on the host cores on bounded slabs of the same workload.
+clock, results read back to the host).  The default line also carries
+`reference_gpu`: the reference's own CUDA backend ("optimized" kernel, built
+unchanged by baseline/build_ref.py) timed on the same GPU in a child process
+before this repository's arm runs.
+
+Reference arms:
+  --impl reference       the reference's own CPU backend (pympcd.Simulation(params,
+                         "cpu") of the unchanged build), one process per host core,
+                         each on a bounded slab of the workload; where that build is
+                         absent, the oracle's restatement of the same step.
+  --impl reference-cuda  the reference's own CUDA backend through
+                         pympcd.Simulation(params, "cuda"): --kernel optimized |
+                         sorting | trivial, --algorithm, --size as for this arm.
 Several GPUs run independent replicas (the step has no exchange).
 """
 from __future__ import annotations
@@ -195,22 +209,206 @@ def cpu_rate(threads: int, warmup: int, steps: int):
     return threads * n * steps / max(times), n
 
 
+def _ref_module_dir(kind: str):
+    """sys.path entry of the reference build `kind` ("stock" or "dropin"), or None."""
+    from baseline import build_ref
+
+    return build_ref.module_dir(kind) if os.path.exists(build_ref.module_path(kind)) else None
+
+
+def _ref_cpu_worker(mod_dir, slab, warmup, steps, barrier, out, i):
+    """One host core: the reference's CPU backend on one slab (spawned process)."""
+    sys.path.insert(0, mod_dir)
+    import pympcd
+
+    p = pympcd.Params()
+    p.n = slab["n"]
+    p.periodicity = slab["periodic"]
+    p.volume_size = (slab["L"][0], slab["L"][1], slab["L"][2] - 2)
+    p.drag = slab["drag"]
+    p.delta_t = slab["dt"]
+    p.temperature = 1.0
+    sim = pympcd.Simulation(p, "cpu")
+    sim.step(warmup)
+    barrier.wait()
+    t0 = time.perf_counter()
+    sim.step(steps)
+    out[i] = time.perf_counter() - t0
+    out[len(out) // 2 + i] = len(sim.get_particle_positions())
+    barrier.wait()
+
+
+def reference_cpu_rate(procs: int, warmup: int, steps: int):
+    """Aggregate particle-steps/s of the reference's own CPU backend: `procs`
+    processes (the backend is single-threaded), each advancing one slab of the
+    workload; None where the reference build is absent."""
+    mod_dir = _ref_module_dir("stock")
+    if mod_dir is None:
+        return None
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(procs + 1)
+    out = ctx.Array("d", 2 * procs)
+    ps = [ctx.Process(target=_ref_cpu_worker, args=(mod_dir, CPU_SLAB, warmup, steps, barrier, out, i))
+          for i in range(procs)]
+    for p in ps:
+        p.start()
+    barrier.wait(timeout=600)
+    barrier.wait(timeout=1800)
+    for p in ps:
+        p.join()
+    if any(p.exitcode != 0 for p in ps):
+        raise RuntimeError("a reference CPU worker failed")
+    times, counts = list(out[:procs]), list(out[procs:])
+    return sum(counts) * steps / max(times), int(counts[0])
+
+
+def cpu_model() -> str:
+    try:
+        import platform
+
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    return f"{platform.machine()} {line.split(':', 1)[1].strip()}"
+        return platform.machine()
+    except Exception:
+        return "unknown"
+
+
+def cpu_baseline_block(warmup: int, steps: int):
+    """cpu_baseline of a line: the reference's CPU backend on every host core,
+    else the oracle's restatement on host threads."""
+    cores = os.cpu_count() or 1
+    slab = (f"{CPU_SLAB['L'][0]}x{CPU_SLAB['L'][1]}x{CPU_SLAB['L'][2] - 2} cells + walls, "
+            f"n={CPU_SLAB['n']}")
+    r = reference_cpu_rate(cores, warmup, steps)
+    if r is not None:
+        rate, n = r
+        return {"value": rate, "unit": UNIT, "cores": cores, "kind": "reference", "cpu": cpu_model(),
+                "sample": f"{cores} processes (one per core; the reference CPU backend is single-threaded), "
+                          f"each one slab of the workload, {slab} ({n} particles), pympcd.Simulation(params, "
+                          f"'cpu') of the unchanged reference build; {warmup} warm-up + {steps} timed steps"}
+    threads = min(cores, 16)
+    rate, n = cpu_rate(threads, warmup, steps)
+    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "cpu": cpu_model(),
+            "sample": f"{threads} threads x one slab, {slab} ({n} particles), the oracle's restatement of "
+                      f"the reference CPU step (reference build absent); {warmup} warm-up + {steps} timed steps"}
+
+
 def run_reference_arm(args, rank):
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
-    rate, n = cpu_rate(threads, args.warmup, args.steps)
-    sample = (f"{threads} independent slabs of the workload, each {CPU_SLAB['L'][0]}x{CPU_SLAB['L'][1]}x"
-              f"{CPU_SLAB['L'][2] - 2} cells + walls, n=20 ({n} particles), advanced by the restated reference "
-              f"CPU step; {args.warmup} warm-up + {args.steps} timed steps")
+    cb = cpu_baseline_block(min(args.warmup, 3), min(args.steps, 20))
+    rate = cb["value"]
     out = {"metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": threads * n / rate * 1e3,
+           "steps": min(args.steps, 20), "warmup": min(args.warmup, 3),
+           "ms_per_step": 4.0e8 / rate * 1e3,   # the whole workload's step at this aggregate rate
            "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": WORKLOAD_NAME, "sample": "per-thread slabs of the same workload"},
-           "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "config": {"workload": WORKLOAD_NAME, "sample": "one slab of the same workload per host core"},
+           "cpu_baseline": cb,
            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+def reference_cuda_workload(args):
+    algorithm = args.algorithm
+    L = tuple(args.size) if args.size else (1000, 1000, 20)
+    if algorithm == "extended" and not args.size:
+        L = (256, 256, 64)
+    n = 20
+    drag = 0.0005 if algorithm == "extended" else 0.001
+    return dict(L=L, n=n, drag=drag, dt=0.02, algorithm=algorithm)
+
+
+def run_reference_cuda(args, rank, local_rank):
+    """The reference's own CUDA backend on this GPU, through its unchanged Python
+    API; host wall clock around step(K) + device synchronisation, as the
+    reference's benchmark.py:53-66 times it, and CUDA events on the default stream
+    the reference launches on."""
+    if rank != 0:
+        return
+    mod_dir = _ref_module_dir("stock")
+    wl = reference_cuda_workload(args)
+    name = (f"reference {args.kernel} {wl['algorithm'].upper()} channel {wl['L'][0]}x{wl['L'][1]}x{wl['L'][2]} "
+            f"cells (+2 wall layers in z), n={wl['n']}, T=1, g={wl['drag']}, dt={wl['dt']}")
+    if mod_dir is None:
+        print(json.dumps({"impl": "reference-cuda", "unavailable": "the reference build (baseline/_ref) is absent"}))
+        return
+    import torch
+
+    sys.path.insert(0, mod_dir)
+    import pympcd
+
+    torch.cuda.set_device(local_rank)
+    p = pympcd.Params()
+    p.n = wl["n"]
+    p.temperature = 1.0
+    p.periodicity = (1, 1, 0)
+    p.volume_size = wl["L"]
+    p.drag = wl["drag"]
+    p.delta_t = wl["dt"]
+    p.algorithm = wl["algorithm"]
+    p.collision_kernel = args.kernel
+    p.device_id = local_rank
+    t0 = time.perf_counter()
+    sim = pympcd.Simulation(p, "cuda")
+    torch.cuda.synchronize()
+    t_init = time.perf_counter() - t0
+    N = len(sim.get_particle_positions())
+    sim.step(args.warmup)
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        t0 = time.perf_counter()
+        start.record()
+        sim.step(args.steps)
+        stop.record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    ev_ms = start.elapsed_time(stop)
+    del sim
+    out = {"metric": METRIC, "value": N * args.steps / wall, "unit": UNIT, "impl": "reference-cuda",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+           "event_ms_per_step": ev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": name, "kernel": args.kernel, "particles": N,
+                      "particles_note": "the reference allocates n x container cells (wall layers included) "
+                                        "and places them all in the fluid (backend_context.cu:19)",
+                      "build": "unchanged reference sources, nvcc sm_103a, -O3 (baseline/build_ref.py)",
+                      "init_s": t_init,
+                      "timing": "host wall clock around step(K) + synchronize (benchmark.py:53-66)"},
+           "clocks": clocks.summary()}
+    print(json.dumps(out), flush=True)
+
+
+def reference_gpu_block(args, local_rank):
+    """The reference's optimized CUDA kernel on the same workload, run in a child
+    process (its memory is released, and a failure there cannot take this
+    process's context with it); None when unavailable."""
+    if _ref_module_dir("stock") is None:
+        return {"unavailable": "the reference build (baseline/_ref) is absent"}
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference-cuda", "--kernel", "optimized",
+           "--steps", str(args.steps), "--warmup", str(args.warmup)]
+    if args.size:
+        cmd += ["--size", *map(str, args.size)]
+    env = dict(os.environ, LOCAL_RANK=str(local_rank), RANK="0", WORLD_SIZE="1")
+    try:
+        proc = subprocess.run(cmd, capture_output=True, text=True, timeout=1200, env=env)
+    except subprocess.TimeoutExpired:
+        return {"unavailable": "the reference arm did not finish within 1200 s"}
+    lines = [l for l in proc.stdout.splitlines() if l.startswith("{")]
+    if proc.returncode != 0 or not lines:
+        return {"unavailable": f"the reference arm failed (rc {proc.returncode}): {proc.stderr.strip()[-300:]}"}
+    r = json.loads(lines[-1])
+    if "unavailable" in r:
+        return r
+    return {"kernel": "optimized", "value": r["value"], "unit": UNIT, "ms_per_step": r["ms_per_step"],
+            "event_ms_per_step": r["event_ms_per_step"], "particles": r["config"]["particles"],
+            "steps": r["steps"], "warmup": r["warmup"], "clocks": r["clocks"],
+            "how": "pympcd.Simulation(params, 'cuda') of the unchanged reference build, same GPU, child process"}
 
 
 # ---------------------------------------------------------------- GPU arm
@@ -251,6 +449,11 @@ def run_gpu_arm(args, rank, world, local_rank):
     import torch
 
     from cudampcd_gb300 import capi
+
+    # the reference's own CUDA kernel on the same GPU, first, in a child process
+    ref_gpu = None
+    if world == 1 and not args.no_reference_gpu:
+        ref_gpu = reference_gpu_block(args, local_rank)
 
     torch.cuda.set_device(local_rank)
     dist = None
@@ -313,13 +516,13 @@ def run_gpu_arm(args, rank, world, local_rank):
             "gpu_launches": 2 * args.steps,   # per step: overflow selection, step kernel
             "device_counters": {"bucket_overflows": overflowed, "error_flags": flags},
         }
+        if ref_gpu is not None:
+            if "value" in ref_gpu:
+                ref_gpu["speedup_ms_per_step"] = ref_gpu["ms_per_step"] / out["ms_per_step"]
+                ref_gpu["speedup_particle_steps"] = value / ref_gpu["value"]
+            out["reference_gpu"] = ref_gpu
         if not args.no_cpu:
-            threads = min(os.cpu_count() or 1, 16)
-            rate, n = cpu_rate(threads, 1, args.steps_cpu)
-            out["cpu_baseline"] = {
-                "value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                "sample": f"{threads} threads x one {CPU_SLAB['L']} slab ({n} particles), "
-                          f"{args.steps_cpu} steps of the restated reference CPU step"}
+            out["cpu_baseline"] = cpu_baseline_block(1, args.steps_cpu)
         print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -479,12 +682,74 @@ def run_viscosity(args):
     print(json.dumps(out), flush=True)
 
 
+def run_adjoint(args):
+    """The differentiable channel (64 x 64 x 32 cells + 2 walls, n = 10, dt = 0.02,
+    200 sampled steps, checkpoints every 20): CUDA-event times of a plain step,
+    of the sampled forward with checkpoints, and of the adjoint; the adjoint's
+    cost relative to a plain step and to the forward."""
+    import math
+
+    import torch
+
+    from cudampcd_gb300 import capi
+    from cudampcd_gb300.adjoint import channel_profile
+
+    L, n, drag0, dt, seed, S, K = (64, 64, 34), 10, 1e-3, 0.02, 5, 200, 20
+    h = capi.Handle(L=L, periodic=(1, 1, 0), n=n, dt=dt, drag=drag0, seed=seed)
+    N = h.N
+    pos = torch.from_numpy(h.positions()).cuda()
+    v_init = torch.from_numpy(h.velocities()).cuda()
+    eta = (1.0 - math.cos(2 * math.pi / 3)) / (18.0 * dt) * (n - 1 + math.exp(-n))
+    hz = L[2] / 2.0 - 1.0
+    z = torch.arange(L[2], dtype=torch.float64, device="cuda") + 0.5 - L[2] / 2.0
+    target = 1.1 * n * drag0 * (hz * hz - z * z) / (2.0 * eta)
+    # plain steps (two launches each), timed on the handle's stream
+    h.step(max(args.warmup, 6))
+    total_ms, _ = h.time_steps(S)
+    plain = total_ms / S
+    fw, bw = [], []
+    for rep in range(1 + 3):   # the first pass pays the one-time setup (tape allocation)
+        v0 = v_init.clone().requires_grad_(True)
+        g = torch.tensor(drag0, dtype=torch.float64, device="cuda", requires_grad=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        U = channel_profile(h, pos, v0, g, S, K)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        loss = ((U[1:-1].double() - target[1:-1]) ** 2).mean()
+        loss.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        if rep:
+            fw.append((t1 - t0) * 1e3 / S)
+            bw.append((t2 - t1) * 1e3 / S)
+        assert torch.isfinite(v0.grad).all()
+    h.close()
+    fwd, bwd = statistics.median(fw), statistics.median(bw)
+    out = {"metric": METRIC, "value": N / (bwd * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": S,
+           "warmup": args.warmup, "ms_per_step": bwd, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"differentiable SRD channel {L[0]}x{L[1]}x{L[2] - 2} cells + 2 walls, n={n}, "
+                                  f"N={N}, dt={dt}, g={drag0}, {S} sampled steps, checkpoints every {K}; loss = MSE "
+                                  f"of U(z) against 1.1 x the analytic parabola; gradients w.r.t. g and all V0",
+                      "timing": "plain steps: CUDA events on the handle's stream; forward and backward: host wall "
+                                "clock around each call (both synchronise), median of 3 after one untimed pass"},
+           "adjoint": {"plain_ms_per_step": plain, "forward_ms_per_step": fwd, "backward_ms_per_step": bwd,
+                       "backward_over_plain": bwd / plain, "backward_over_forward": bwd / fwd,
+                       "forward_plus_backward_over_plain": (fwd + bwd) / plain,
+                       "value_meaning": "value = particle-steps/s of the adjoint (backward) sweep"}}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=100)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference", "reference-cuda"])
+    ap.add_argument("--kernel", default="optimized", choices=["optimized", "sorting", "trivial"])
+    ap.add_argument("--no-reference-gpu", dest="no_reference_gpu", action="store_true")
+    ap.add_argument("--adjoint", action="store_true")
     ap.add_argument("--steps-cpu", dest="steps_cpu", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -500,7 +765,9 @@ def main():
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
-    if args.ensemble:
+    if args.adjoint:
+        run_adjoint(args)
+    elif args.ensemble:
         run_ensemble(args)
     elif args.physics == "viscosity":
         run_viscosity(args)
@@ -508,6 +775,8 @@ def main():
         run_physics(args)
     elif args.impl == "reference":
         run_reference_arm(args, rank)
+    elif args.impl == "reference-cuda":
+        run_reference_cuda(args, rank, local_rank)
     else:
         run_gpu_arm(args, rank, world, local_rank)
 

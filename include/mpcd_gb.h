@@ -7,7 +7,7 @@
  * mpcd::create_backend(params, "cuda") (src/libmpcd/common/backend_factory.hpp:15-27)
  * for mpcd::api::SimulationHandle (src/libmpcd/api/simulator_handle.cpp:9).
  * Every Backend member maps onto one function below; a Backend subclass that
- * forwards to them is all the reference tree needs (see INTEGRATION.md).
+ * forwards to them is all the reference tree needs.
  *
  * Conventions
  *   - plain pointers and sizes; host buffers unless a name says "device";

@@ -4,8 +4,10 @@
   any machine with gcc.
 * ``oracle/_ref/libmpcd_ref.so`` -- ``oracle/ref_harness.cpp`` compiled with the
   reference's own CPU sources, read where they lie in the reference tree.  Built
-  only where that tree exists (``MPCD_REFERENCE_ROOT``, default
-  ``/root/reference``); the output stays out of version control.
+  only where that tree exists: ``MPCD_REFERENCE_ROOT``, else a checkout named
+  ``reference`` beside this repository, else the copy that
+  ``baseline/build_ref.py`` staged in ``baseline/_ref/tree``; the output stays
+  out of version control.
 
 Flags: the reference's Release build (``-O3 -DNDEBUG``, C++17) for the harness;
 ``-ffp-contract=off`` everywhere so that no multiply-add is fused (GCC fuses by
@@ -18,7 +20,21 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("MPCD_REFERENCE_ROOT", "/root/reference")
+_CPU_SRC = os.path.join("src", "libmpcd", "cpu_backend", "simulation_functions.cpp")
+
+
+def _find_ref_root() -> str:
+    env = os.environ.get("MPCD_REFERENCE_ROOT")
+    if env:
+        return env
+    repo = os.path.dirname(HERE)
+    for cand in (os.path.join(os.path.dirname(repo), "reference"), os.path.join(repo, "baseline", "_ref", "tree")):
+        if os.path.isfile(os.path.join(cand, _CPU_SRC)):
+            return cand
+    return os.path.join(os.path.dirname(repo), "reference")
+
+
+REF_ROOT = _find_ref_root()
 
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libmpcd_ref.so")
@@ -48,7 +64,7 @@ def build_oracle(force: bool = False) -> str:
 
 
 def reference_available() -> bool:
-    return os.path.isfile(os.path.join(REF_ROOT, "src", "libmpcd", "cpu_backend", "simulation_functions.cpp"))
+    return os.path.isfile(os.path.join(REF_ROOT, _CPU_SRC))
 
 
 def build_ref(force: bool = False) -> str | None:

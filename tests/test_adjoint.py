@@ -151,12 +151,17 @@ def test_adjoint_matches_central_differences_with_common_random_numbers():
     which no discrete event flips -- checked by comparing the full event tapes of
     the runs.  The map is then affine and the loss quadratic, so central
     differences are exact up to FP32 rounding.  A small box and a short horizon
-    keep event flips rare at perturbations FP32 still resolves.  The sampled
-    profile sums velocities with float atomics, whose rounding varies from run to
-    run (by up to about 3e-4 of the velocity difference quotient at the largest
-    event-preserving perturbation), so each loss is the mean of three runs and the
-    bound is 2e-3 (measured 4e-4 to 7e-4); the FP64 autograd test above pins the adjoint itself (to 1e-4,
-    measured 6e-7)."""
+    keep event flips rare at perturbations FP32 still resolves.
+
+    The noise floor of a difference quotient is the FP32 profile: U is returned in
+    float32 and its per-step cell sums are float atomics whose rounding varies from
+    run to run, a few 1e-9 absolute on a profile of a few 1e-2.  The velocity
+    direction is therefore chosen to move the loss as much as the event budget
+    allows: eight particles, each component perturbed along the sign of the
+    adjoint's own gradient (so dL/dV0 . delta = sum |dL/dV0_ij| over them, first
+    order in any error of the adjoint, not a random projection), and each loss is
+    the mean of five runs.  Bound 1e-3 on both gradients; the FP64 autograd test
+    above pins the adjoint itself (to 1e-4, measured 6e-7)."""
     L, n, drag0, dt, seed, S, K = (4, 4, 6), 10, 1e-3, 0.02, 9, 12, 4
     h = capi.Handle(L=L, periodic=(1, 1, 0), n=n, dt=dt, drag=drag0, seed=seed)
     try:
@@ -169,7 +174,7 @@ def test_adjoint_matches_central_differences_with_common_random_numbers():
         _, tape0 = _loss_and_tape(h, pos, base_v, drag0, S, K, target)
 
         def mean_loss(v, drag):
-            runs = [_loss_and_tape(h, pos, v, drag, S, K, target) for _ in range(3)]
+            runs = [_loss_and_tape(h, pos, v, drag, S, K, target) for _ in range(5)]
             same = all(_same_events(t, tape0) for _, t in runs)
             return float(np.mean([l for l, _ in runs])), same
 
@@ -187,14 +192,14 @@ def test_adjoint_matches_central_differences_with_common_random_numbers():
         gen = torch.Generator(device="cuda").manual_seed(3)
         delta = torch.zeros_like(base_v)
         who = torch.randperm(h.N, generator=gen, device="cuda")[:8]
-        delta[who] = torch.randn((8, 3), device="cuda", generator=gen)
+        delta[who] = torch.sign(v0.grad[who])
         fd_v, eps_v = central(lambda e: (base_v + e * delta, drag0), [2e-2, 1e-2, 5e-3, 2e-3, 1e-3, 5e-4])
         ad_v = (v0.grad * delta).sum().item()
         err_v = abs(ad_v - fd_v) / abs(fd_v)
         print(f"central differences: dL/dg adjoint {g.grad.item():.6e} FD {fd_g:.6e} (eps {eps_g:g}) rel {err_g:.2e}; "
               f"dL/dV0 . delta adjoint {ad_v:.6e} FD {fd_v:.6e} (eps {eps_v:g}) rel {err_v:.2e}")
-        assert err_g < 2e-3
-        assert err_v < 2e-3
+        assert err_g < 1e-3
+        assert err_v < 1e-3
     finally:
         h.close()
 

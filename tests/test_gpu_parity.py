@@ -263,3 +263,59 @@ def test_extreme_densities_and_thin_boxes_match_oracle(name):
     h.step(5)   # and keeps stepping without device errors
     assert h.counters()[1] == 0
     h.close()
+
+
+# Boxes large enough that every CTA of the persistent step kernel (4 per SM x 152
+# SMs) sweeps many tiles: the next-tile locator, the one-tile-ahead count prefetch,
+# the in-sweep clearing of the previous step's counts and the overflow chains all
+# run as in production.  (box, production steps compared)
+MULTI_TILE = {
+    # 160 x 160 x 20 fluid layers + 2 walls, n = 20: 563,200 cells, 8,800 tiles of 64
+    # cells, about 14 per CTA
+    "srd_160x160x20": (O.Box(L=(160, 160, 22), periodic=(1, 1, 0), algorithm=O.SRD, n=20, dt=0.02, drag=0.001), 3),
+    # extended, 100 x 100 x 20 + 2 walls: 220,000 cells in 64-cell tiles
+    "ext_100x100x20": (O.Box(L=(100, 100, 22), periodic=(1, 1, 0), algorithm=O.EXTENDED, n=20, dt=0.02,
+                             drag=0.0005), 2),
+    # n = 1 over 200 x 200 x 10 + 2 walls: 480,000 cells in 128-cell tiles, and
+    # cells that receive more than 4n particles in most tiles
+    "srd_sparse_200x200x10": (O.Box(L=(200, 200, 12), periodic=(1, 1, 0), algorithm=O.SRD, n=1, dt=0.05,
+                                    drag=0.01), 3),
+}
+
+
+@pytest.mark.parametrize("name", list(MULTI_TILE))
+def test_multi_tile_production_steps_match_oracle(name):
+    """Consecutive production steps of a large box, each compared with the oracle's
+    restatement of the reference step (Philox draw model) applied to the GPU's own
+    state before it: positions and velocities of every particle within 1e-5.  In
+    the extended collision, a gate draw within FP32 rounding of its probability can
+    flip between the GPU's fixed-tree sums and the oracle's sequential ones; the
+    particles off by more than the tolerance must then all share one collision cell."""
+    box, steps = MULTI_TILE[name]
+    seed = 4242
+    h = make(box, seed=seed)
+    try:
+        pos, vel, _ = O.distribute(box, h.N, 13, 14)
+        set_state(h, pos, vel)
+        overflowed = False
+        for _ in range(steps):
+            k = h.step_index
+            s0 = h.shift(k)
+            h.step(1)
+            gp, gv = h.positions(), h.velocities()
+            tp, tv, tc, counter, table = O.translate(box, pos, vel, s0)
+            overflowed |= bool((counter > 4 * box.n).any())
+            op, ov, _ = O.collide(box, tp, tv, tc, counter, table, s0, O.Draws.empty(box), O.DRAWS_PHILOX,
+                                  seed=seed, step=k)
+            assert rel_err(gp, op, 1.0).max() <= REL_TOL
+            bad = (rel_err(gv, ov, box.thermal_velocity) > REL_TOL).any(axis=1)
+            if box.algorithm == O.EXTENDED:
+                assert len(np.unique(tc[bad])) <= 1, f"step {k}: {bad.sum()} particles in several cells differ"
+            else:
+                assert not bad.any(), f"step {k}: {bad.sum()} particles differ"
+            pos, vel = gp, gv
+        assert h.counters()[1] == 0
+        if box.n == 1:
+            assert overflowed and h.counters()[0] > 0
+    finally:
+        h.close()
