@@ -31,7 +31,7 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1
 }
 
 // Draw purposes; counter = {a, step_lo, purpose | step_hi << 8, d}, key = box seed.
-enum : uint32_t { kShift = 1, kAxis = 2, kGhostCount = 3, kGhost = 4, kThermal = 5, kInit = 6 };
+enum : uint32_t { kShift = 1, kAxis = 2, kGhostCount = 3, kGhost = 4, kThermal = 5, kInit = 6, kGhostSum = 7 };
 
 __device__ __forceinline__ uint4 draw(const BoxDesc& b, uint64_t step, uint32_t purpose, uint32_t a, uint32_t d)
 {

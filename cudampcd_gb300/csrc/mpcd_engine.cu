@@ -803,7 +803,7 @@ private:
     void build_boxes()
     {
         boxes_.clear();
-        uint64_t cells = 0, slots = 0, particles = 0;
+        uint64_t cells = 0, slots = 0, particles = 0, walls = 0;
         uint32_t n_max = 0;
         for (const mpcd_gb_params& p : box_params_) {
             BoxDesc b = make_box(p);
@@ -811,6 +811,8 @@ private:
             b.cell_base = (uint32_t)cells;
             b.slot_base = slots;
             b.dense_base = particles;
+            b.wall_base = walls;
+            if (b.wall_z) walls += 2ull * (uint64_t)b.L[0] * (uint64_t)b.L[1];
             cells += b.C;
             slots += (uint64_t)b.C * b.cap;
             particles += b.N;
@@ -820,6 +822,7 @@ private:
         if (particles >= (1ull << 32) - 1) throw Error(MPCD_GB_EINVAL, "too many particles in the ensemble");
         N_ = particles;
         cells_ = cells;
+        walls_ = walls;
         total_slots_ = slots;
         ov_cap_ = (uint32_t)std::max<uint64_t>(1u << 16, std::min<uint64_t>(N_, 1u << 22));
         if (total_slots_ + ov_cap_ >= (1ull << 32))
@@ -922,8 +925,7 @@ private:
         check(boxes_d_.alloc(sizeof(BoxDesc) * boxes_.size()), "alloc boxes");
         upload_tiling();
         for (int k = 0; k < 2; ++k) {
-            check(pos_[k].alloc(sizeof(float4) * total_slots_), "alloc bucket positions");
-            check(vel_[k].alloc(sizeof(float4) * total_slots_), "alloc bucket velocities");
+            check(slots_[k].alloc(sizeof(Slot) * total_slots_), "alloc buckets");
             check(ov_pos_[k].alloc(sizeof(float4) * ov_cap_), "alloc overflow list");
             check(ov_vel_[k].alloc(sizeof(float4) * ov_cap_), "alloc overflow list");
             check(ov_next_[k].alloc(sizeof(uint32_t) * ov_cap_), "alloc overflow chains");
@@ -933,6 +935,7 @@ private:
             check(count_[k].alloc(sizeof(uint32_t) * cells_), "alloc counts");
             check(cudaMemset(count_[k].p, 0, count_[k].bytes), "clear counts");
         }
+        if (walls_) check(ghosts_.alloc(sizeof(GhostSum) * walls_), "alloc wall ghosts");
         check(state_.alloc(sizeof(DeviceState)), "alloc state");
         check(cudaMemset(state_.p, 0, sizeof(DeviceState)), "clear state");
         check(samp_.alloc(sizeof(float4) * cells_), "alloc sample");
@@ -1001,11 +1004,9 @@ private:
         a.total_slots = total_slots_;
         a.step = k;
         const unsigned p = (unsigned)(k & 1), q = p ^ 1u;
-        a.in_pos = pos_[p].as<float4>();
-        a.in_vel = vel_[p].as<float4>();
+        a.in_slots = slots_[p].as<Slot>();
         a.in_count = count_[k % 3].as<uint32_t>();
-        a.out_pos = pos_[q].as<float4>();
-        a.out_vel = vel_[q].as<float4>();
+        a.out_slots = slots_[q].as<Slot>();
         a.out_count = count_[(k + 1) % 3].as<uint32_t>();
         a.zero_count = count_[(k + 2) % 3].as<uint32_t>();
         a.ov_in_pos = ov_pos_[p].as<float4>();
@@ -1067,6 +1068,7 @@ private:
             StepArgs a = args((uint64_t)i);   // buffers of step i == those of any step = i mod 6
             a.step_base = step_base_ptr();
             a.sample = sample ? 1 : 0;
+            use_run_kernel_ghosts(a, false);
             err = select_overflow(a, (uint64_t)i, cs);
             if (err == cudaSuccess) err = launch_step(a, params_.algorithm, false, pbuf_, grid_, cs);
             if (err == cudaSuccess && sample)
@@ -1105,8 +1107,16 @@ private:
     cudaError_t select_overflow(const StepArgs& a, uint64_t k, cudaStream_t st)
     {
         const unsigned p = (unsigned)(k & 1);
-        return launch_overflow_select(a, pos_[p].as<float4>(), vel_[p].as<float4>(), ov_pos_[p].as<float4>(),
-                                      ov_vel_[p].as<float4>(), sms_, st);
+        return launch_overflow_select(a, slots_[p].as<Slot>(), ov_pos_[p].as<float4>(), ov_vel_[p].as<float4>(),
+                                      a.ghosts ? sms_ * 8 : sms_, st);
+    }
+
+    // The wall-ghost array of srd_run_kernel for a step that it runs (its prologue
+    // draws the ghosts), else none.
+    void use_run_kernel_ghosts(StepArgs& a, bool table) const
+    {
+        a.ghosts = ghosts_.as<GhostSum>();
+        if (!run_kernel_takes(a, params_.algorithm, table)) a.ghosts = nullptr;
     }
 
     // One step: the overflow selection, then the step kernel (bracketed by the
@@ -1115,6 +1125,7 @@ private:
     {
         StepArgs a = args(step_);
         a.sample = sample ? 1 : 0;
+        use_run_kernel_ghosts(a, use_table_);
         check(select_overflow(a, step_, stream_), "overflow selection");
         if (before) check(cudaEventRecord(before, stream_), "event");
         check(launch_step(a, params_.algorithm, use_table_, pbuf_, grid_, stream_), "step kernel");
@@ -1207,7 +1218,7 @@ private:
     {
         const unsigned p = parity();
         StepArgs a = args(step_);
-        check(launch_layout(a, count_[step_ % 3].as<uint32_t>(), pos_[p].as<float4>(), vel_[p].as<float4>(),
+        check(launch_layout(a, count_[step_ % 3].as<uint32_t>(), slots_[p].as<Slot>(),
                             offsets_.as<uint32_t>(), cells_, N_, scan_status_.as<unsigned long long>(),
                             scan_counter_.as<unsigned int>(), ov_pos_[p].as<float4>(), ov_vel_[p].as<float4>(),
                             (unsigned)(step_ % 3), cell, slot, prev, id, sms_ * 8, stream_),
@@ -1268,7 +1279,7 @@ private:
     cudaStream_t own_stream_ = nullptr, stream_ = nullptr;
     int sms_ = 0, grid_ = 0;
     std::vector<BoxDesc> boxes_;
-    uint64_t N_ = 0, cells_ = 0, tiles_ = 0, total_slots_ = 0;
+    uint64_t N_ = 0, cells_ = 0, tiles_ = 0, total_slots_ = 0, walls_ = 0;
     uint32_t ov_cap_ = 0, pbuf_ = 0;
     uint32_t max_tile_cells_ = 0, forced_tile_cells_ = 0;   // largest tile of any box; a tile size forced for all
     double fill_ = 1.0;                                      // expected particles per tile = pbuf / fill
@@ -1287,7 +1298,7 @@ private:
     std::vector<TileEntry> tile_info_;   // tile table of the current tiling
     DeviceBuffer tile_info_d_;
     DeviceBuffer ov_head_[2], ov_next_[2];   // overflow chains: heads by cell, links by entry (by step parity)
-    DeviceBuffer boxes_d_, pos_[2], vel_[2], count_[3], ov_pos_[2], ov_vel_[2], state_, samp_, acc_, dense_pos_,
+    DeviceBuffer boxes_d_, slots_[2], ghosts_, count_[3], ov_pos_[2], ov_vel_[2], state_, samp_, acc_, dense_pos_,
         dense_vel_, offsets_, scan_status_, scan_counter_, partial_;
     DeviceBuffer t_count_, t_gpos_, t_gvel_, t_axis_, t_gate_, t_gauss_;
     // adjoint: checkpoints, tape of one segment, adjoint state

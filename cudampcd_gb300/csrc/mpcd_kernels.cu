@@ -101,6 +101,14 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// One bucket slot (32 bytes, a full sector) with a single 256-bit store.
+__device__ __forceinline__ void store_slot(Slot* dst, float4 p, float4 v)
+{
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(dst), "f"(p.x), "f"(p.y), "f"(p.z),
+                 "f"(p.w), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+
 __device__ __forceinline__ unsigned lanemask_lt()
 {
     unsigned m;
@@ -196,9 +204,7 @@ __device__ __forceinline__ void store_particle(const StepArgs& a, const BoxDesc&
     if (!active) return;
     const float4 xp = make_float4(xs.x, xs.y, xs.z, 0.0f), vp = make_float4(vs.x, vs.y, vs.z, __uint_as_float(id));
     if (slot < b.cap) {
-        const uint64_t at = b.slot_base + (uint64_t)(key - b.cell_base) * b.cap + slot;
-        a.out_pos[at] = xp;
-        a.out_vel[at] = vp;
+        store_slot(a.out_slots + b.slot_base + (uint64_t)(key - b.cell_base) * b.cap + slot, xp, vp);
     } else {
         push_overflow(a, key, xp, vp);
     }
@@ -215,6 +221,78 @@ __device__ __forceinline__ float3 srd_axis_philox(const BoxDesc& b, uint64_t ste
     float s, c;
     sincospif(2.0f * u01(o.y), &s, &c);
     return make_float3(rho * c, rho * s, z);
+}
+
+// Velocity of wall ghost j of cell `ref` (Maxwell-Boltzmann, sqrt(T) per component).
+__device__ __forceinline__ float3 ghost_velocity(const BoxDesc& b, uint64_t step, uint32_t ref, uint32_t j)
+{
+    const uint4 o = draw(b, step, kGhost, ref, 2 * j + 1);
+    float g0, g1, g2, g3;
+    box_muller(o.x, o.y, g0, g1);
+    box_muller(o.z, o.w, g2, g3);
+    return make_float3(g0 * b.tv, g1 * b.tv, g2 * b.tv);
+}
+
+// Total velocity of the g wall ghosts of cell `ref` for the SRD collision, which
+// uses the ghosts only through their sum: g independent Maxwell-Boltzmann
+// velocities sum to one Gaussian of variance g T per component, drawn here once
+// per cell (the reference draws each ghost, srd_collision_strategy.cu:79-94; the
+// extended collision, which uses each ghost's position, still draws them one by one).
+__device__ __forceinline__ float3 ghost_sum_velocity(const BoxDesc& b, uint64_t step, uint32_t ref, uint32_t g)
+{
+    const uint4 o = draw(b, step, kGhostSum, ref, 0);
+    float g0, g1, g2, g3;
+    box_muller(o.x, o.y, g0, g1);
+    box_muller(o.z, o.w, g2, g3);
+    const float sc = sqrtf((float)g) * b.tv;
+    return make_float3(g0 * sc, g1 * sc, g2 * sc);
+}
+
+// SRD cell sums are exact: each velocity component is rounded to a multiple of
+// 2^-24 and the multiples are summed as 64-bit integers, so the sum depends
+// neither on the order of the bucket (the arrival order of the claims) nor on
+// how it is split.  round(v 2^24) of any v, converted to 64 bits:
+constexpr float kFixScale = 16777216.0f;   // 2^24
+__device__ __forceinline__ long long fixed24(float v) { return __float2ll_rn(v * kFixScale); }
+
+// The same value through the 32-bit conversion (the 64-bit one runs on the
+// narrow FP64 pipe); exact while |v| < 32, and the largest magnitude converted
+// is tracked in `mx` so that a caller can redo its sums with fixed24 when it
+// reaches 2^29 (|v| >= 32, or a saturated conversion).
+__device__ __forceinline__ int fixed24_narrow(float v, unsigned& mx)
+{
+    const int r = __float2int_rn(v * kFixScale);
+    mx = max(mx, r < 0 ? 0u - (unsigned)r : (unsigned)r);
+    return r;
+}
+constexpr unsigned kNarrowLimit = 1u << 29;   // four narrow values still sum in 32 bits
+
+// Mean velocity of a cell of n > 1 entries (particles and ghosts) from its exact sums.
+__device__ __forceinline__ float3 srd_mean(long long sx, long long sy, long long sz, uint32_t n)
+{
+    const float inv = 1.0f / (float)n;
+    return make_float3((__ll2float_rn(sx) * 0x1p-24f) * inv, (__ll2float_rn(sy) * 0x1p-24f) * inv,
+                       (__ll2float_rn(sz) * 0x1p-24f) * inv);
+}
+
+// SRD collision of one particle of a cell of more than one entry (srd_collision,
+// simulation_functions.cpp:108-202): v' = u + v_par + cos a v_perp + sin a (v_perp x axis)
+// with fused multiply-adds (compared to 1e-5, not bit-exactly), then the grid shift
+// undone, x = pbc(x - s) (the staged x is wrapped and |s| <= 1/2), and the drag.
+__device__ __forceinline__ void srd_collide(const BoxDesc& b, float3 s, float3 mean, float3 axis, float3& x, float3& v)
+{
+    const float3 vr = make_float3(v.x - mean.x, v.y - mean.y, v.z - mean.z);
+    const float vd = __fmaf_rn(vr.x, axis.x, __fmaf_rn(vr.y, axis.y, vr.z * axis.z));
+    const float3 vpara = make_float3(axis.x * vd, axis.y * vd, axis.z * vd);
+    const float3 vperp = make_float3(vr.x - vpara.x, vr.y - vpara.y, vr.z - vpara.z);
+    const float3 cr = make_float3(__fmaf_rn(vperp.y, axis.z, -(vperp.z * axis.y)),
+                                  __fmaf_rn(vperp.z, axis.x, -(vperp.x * axis.z)),
+                                  __fmaf_rn(vperp.x, axis.y, -(vperp.y * axis.x)));
+    v = make_float3(__fmaf_rn(b.sin_a, cr.x, __fmaf_rn(b.cos_a, vperp.x, vpara.x)) + mean.x,
+                    __fmaf_rn(b.sin_a, cr.y, __fmaf_rn(b.cos_a, vperp.y, vpara.y)) + mean.y,
+                    __fmaf_rn(b.sin_a, cr.z, __fmaf_rn(b.cos_a, vperp.z, vpara.z)) + mean.z);
+    x = pbc_near(b, make_float3(x.x - s.x, x.y - s.y, x.z - s.z));
+    v.x += b.drag_dt;
 }
 
 template <bool TABLE>
@@ -237,15 +315,11 @@ struct Draws<false> {   // Philox (production)
     __device__ static void ghost(const StepArgs&, const BoxDesc& b, uint64_t step, uint32_t ref, uint32_t j,
                                  float3 centre, float shift, bool layer, bool sign, float3& x, float3& v)
     {
-        uint4 o = draw(b, step, kGhost, ref, 2 * j);
+        const uint4 o = draw(b, step, kGhost, ref, 2 * j);
         const float uz = u01(o.z);
         const float z = (layer ^ sign) ? shift * uz : shift + (1.0f - shift) * uz;
         x = make_float3((u01(o.x) - 0.5f) + centre.x, (u01(o.y) - 0.5f) + centre.y, (z - 0.5f) + centre.z);
-        o = draw(b, step, kGhost, ref, 2 * j + 1);
-        float g0, g1, g2, g3;
-        box_muller(o.x, o.y, g0, g1);
-        box_muller(o.z, o.w, g2, g3);
-        v = make_float3(g0 * b.tv, g1 * b.tv, g2 * b.tv);
+        v = ghost_velocity(b, step, ref, j);
     }
     __device__ static float3 srd_axis(const StepArgs&, const BoxDesc& b, uint64_t step, uint32_t ref)
     {
@@ -349,14 +423,14 @@ constexpr uint32_t kGhostFlag = 0x8000u;   // s_cell entries of ghost particles 
 constexpr int kMaxPerThread = 8;   // particle buffer <= kMaxPerThread * kThreads
 
 // Shared memory of one CTA, carved from the dynamic allocation:
-//   particles: pos (float4; after the collision pass .w holds the next cell key),
-//              vel (float4), cell (u16)
+//   particles: slots (pos, vel: the bucket layout, so that a cell is one bulk
+//              copy; after the collision pass pos.w holds the next cell key),
+//              cell (u16)
 //   extended only: rank (u16), stable index (u16)
 //   cells: cnt, ng, off, goff (u32, T + 1 each), c0, c1 (float4, T each)
 //   extended only: omega (float4, T)
 struct TileLayout {
-    float4* pos;
-    float4* vel;
+    Slot* buf;
     uint16_t* cell;
     uint16_t* rank;
     uint16_t* inv;
@@ -376,9 +450,8 @@ __host__ __device__ inline size_t tile_smem_bytes(uint32_t pbuf, uint32_t cells,
 __device__ inline TileLayout carve(unsigned char* base, uint32_t pbuf, uint32_t cells, int algorithm)
 {
     TileLayout t;
-    t.pos = reinterpret_cast<float4*>(base);
-    t.vel = t.pos + pbuf;
-    t.cell = reinterpret_cast<uint16_t*>(t.vel + pbuf);
+    t.buf = reinterpret_cast<Slot*>(base);
+    t.cell = reinterpret_cast<uint16_t*>(t.buf + pbuf);
     t.rank = t.cell + pbuf;
     t.inv = t.rank + (algorithm ? pbuf : 0);
     size_t at = (size_t)pbuf * (16 + 16 + 2 + (algorithm ? 4 : 0));
@@ -496,8 +569,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
     __shared__ float3 sshift[2];
     const uint32_t tcells = a.boxes_tile_cells;   // the largest tile of the launch (boxes may use smaller ones)
     const TileLayout L = carve(dyn, pbuf, tcells, ALGO);
-    float4* const s_pos = L.pos;
-    float4* const s_vel = L.vel;
+    Slot* const s_buf = L.buf;
     uint16_t* const s_cell = L.cell;
     uint16_t* const s_rank = L.rank;   // extended only
     uint16_t* const s_inv = L.inv;     // extended only
@@ -667,7 +739,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                 return;
             }
 
-            // stage real particles: one bulk copy per cell and array
+            // stage real particles: one bulk copy per cell
             const uint32_t real_bytes = 32u * (np - (L.goff[i1] - L.goff[i0]));
             if (!(s_armed && i0 == 0)) {   // not armed by the scan warp: this sub-tile arms its own
                 if (tid == 0 && real_bytes) {
@@ -684,8 +756,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                 if (leader && n) {
                     fence_proxy_async();
                     const uint64_t src = b.slot_base + (uint64_t)(c0 + i) * b.cap;
-                    bulk_g2s(s_pos + o, a.in_pos + src, n * 16u, &bar);
-                    bulk_g2s(s_vel + o, a.in_vel + src, n * 16u, &bar);
+                    bulk_g2s(s_buf + o, a.in_slots + src, n * 32u, &bar);
                 }
                 for (uint32_t p = o + my_j; p < e; p += G)   // cell of the entry, kGhostFlag on ghosts
                     s_cell[p] = (uint16_t)(i | (p - o >= n ? kGhostFlag : 0u));
@@ -704,10 +775,15 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                     bool layer, ghosts;
                     wall_layer(b, cc.z, sign, layer, ghosts);
                     float3 gx, gv;
-                    D::ghost(a, b, step, ref_index(b, cc), j, cell_centre(b, cc), shift_abs, layer, sign, gx, gv);
+                    if (ALGO == 0 && !TABLE) {   // SRD: the ghosts' summed velocity on the first, zero on the rest
+                        gx = cell_centre(b, cc);
+                        gv = j == 0 ? ghost_sum_velocity(b, step, ref_index(b, cc), L.ng[i]) : make_float3(0, 0, 0);
+                    } else {
+                        D::ghost(a, b, step, ref_index(b, cc), j, cell_centre(b, cc), shift_abs, layer, sign, gx, gv);
+                    }
                     const uint32_t p = L.off[i] - pbase + L.cnt[i] + j;
-                    s_pos[p] = make_float4(gx.x, gx.y, gx.z, 0.0f);
-                    s_vel[p] = make_float4(gv.x, gv.y, gv.z, 0.0f);
+                    s_buf[p].pos = make_float4(gx.x, gx.y, gx.z, 0.0f);
+                    s_buf[p].vel = make_float4(gv.x, gv.y, gv.z, 0.0f);
                 }
             }
             if (real_bytes) {
@@ -735,9 +811,9 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                     const uint32_t o = L.off[ci] - pbase;
                     const uint32_t n = L.cnt[ci];
                     if (!(info & kGhostFlag)) {
-                        const uint32_t id = __float_as_uint(s_vel[p].w);
+                        const uint32_t id = __float_as_uint(s_buf[p].vel.w);
                         uint32_t rank = 0;
-                        for (uint32_t q = 0; q < n; ++q) rank += __float_as_uint(s_vel[o + q].w) < id;
+                        for (uint32_t q = 0; q < n; ++q) rank += __float_as_uint(s_buf[o + q].vel.w) < id;
                         s_rank[p] = (uint16_t)rank;
                         s_inv[o + rank] = (uint16_t)p;
                     }
@@ -749,7 +825,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
             // drag, lab-grid sample, stream step k+1 and find the next cell.  k0 = (mean,
             // n), k1 = (axis or centre of mass, wall side) of the particle's cell ci.
             auto finish = [&](uint32_t p, uint32_t ci, const float4 k0, const float4 k1) {
-                const float4 xp = s_pos[p], vp = s_vel[p];
+                const float4 xp = s_buf[p].pos, vp = s_buf[p].vel;
                 float3 x = make_float3(xp.x, xp.y, xp.z);
                 float3 v = make_float3(vp.x, vp.y, vp.z);
                 const uint32_t n = __float_as_uint(k0.w);
@@ -757,21 +833,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                 bool collided = false;
                 if (ALGO == 0) {
                     if (n > 1) {
-                        // v' = u + v_par + cos a v_perp + sin a (v_perp x axis), with fused
-                        // multiply-adds (the collision is compared to 1e-5, not bit-exactly)
-                        const float3 axis = make_float3(k1.x, k1.y, k1.z);
-                        const float3 vr = make_float3(v.x - mean.x, v.y - mean.y, v.z - mean.z);
-                        const float vd = __fmaf_rn(vr.x, axis.x, __fmaf_rn(vr.y, axis.y, vr.z * axis.z));
-                        const float3 vpara = make_float3(axis.x * vd, axis.y * vd, axis.z * vd);
-                        const float3 vperp = make_float3(vr.x - vpara.x, vr.y - vpara.y, vr.z - vpara.z);
-                        const float3 cr = make_float3(__fmaf_rn(vperp.y, axis.z, -(vperp.z * axis.y)),
-                                                      __fmaf_rn(vperp.z, axis.x, -(vperp.x * axis.z)),
-                                                      __fmaf_rn(vperp.x, axis.y, -(vperp.y * axis.x)));
-                        v = make_float3(__fmaf_rn(b.sin_a, cr.x, __fmaf_rn(b.cos_a, vperp.x, vpara.x)) + mean.x,
-                                        __fmaf_rn(b.sin_a, cr.y, __fmaf_rn(b.cos_a, vperp.y, vpara.y)) + mean.y,
-                                        __fmaf_rn(b.sin_a, cr.z, __fmaf_rn(b.cos_a, vperp.z, vpara.z)) + mean.z);
-                        x = pbc_near(b, make_float3(x.x - s.x, x.y - s.y, x.z - s.z));   // staged x is wrapped
-                        v.x += b.drag_dt;
+                        srd_collide(b, s, mean, make_float3(k1.x, k1.y, k1.z), x, v);
                         collided = true;
                     }
                 } else {
@@ -810,8 +872,8 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                     if (b.wall_z && vn.z != v.z) imp[v.z > 0.0f ? 1 : 0] += 2.0f * fabsf(v.z);   // bounce-back
                 }
                 const uint32_t next = b.cell_base + storage_index(b, cell_of_wrapped(b, xn));
-                s_pos[p] = make_float4(xn.x, xn.y, xn.z, __uint_as_float(next));
-                s_vel[p] = make_float4(vn.x, vn.y, vn.z, vp.w);
+                s_buf[p].pos = make_float4(xn.x, xn.y, xn.z, __uint_as_float(next));
+                s_buf[p].vel = make_float4(vn.x, vn.y, vn.z, vp.w);
                 const bool need_lab = a.sample || (ALGO == 0 && a.tape_key);
                 const uint32_t lab = need_lab ? b.cell_base + storage_index(b, cell_of_wrapped(b, x)) : 0u;
                 if (ALGO == 0 && a.tape_key) {
@@ -824,7 +886,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
             };
 
             if (ALGO == 0) {
-                // SRD: exact velocity sum of each cell (2^-32 fixed point, independent of
+                // SRD: exact velocity sum of each cell (2^-24 fixed point, independent of
                 // bucket order; ghosts included), one group per cell
                 const uint32_t i = my_cell;
                 const uint32_t o = in_sub ? L.off[i] - pbase : 0;
@@ -832,19 +894,19 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                 long long sx = 0, sy = 0, sz = 0, tx = 0, ty = 0, tz = 0;   // two chains (integer: exact)
                 uint32_t q = my_j;
                 for (; q + G < n; q += 2 * G) {
-                    const float4 va = s_vel[o + q], vb = s_vel[o + q + G];
-                    sx += __float2ll_rn(va.x * 4294967296.0f);
-                    sy += __float2ll_rn(va.y * 4294967296.0f);
-                    sz += __float2ll_rn(va.z * 4294967296.0f);
-                    tx += __float2ll_rn(vb.x * 4294967296.0f);
-                    ty += __float2ll_rn(vb.y * 4294967296.0f);
-                    tz += __float2ll_rn(vb.z * 4294967296.0f);
+                    const float4 va = s_buf[o + q].vel, vb = s_buf[o + q + G].vel;
+                    sx += fixed24(va.x);
+                    sy += fixed24(va.y);
+                    sz += fixed24(va.z);
+                    tx += fixed24(vb.x);
+                    ty += fixed24(vb.y);
+                    tz += fixed24(vb.z);
                 }
                 if (q < n) {
-                    const float4 va = s_vel[o + q];
-                    sx += __float2ll_rn(va.x * 4294967296.0f);
-                    sy += __float2ll_rn(va.y * 4294967296.0f);
-                    sz += __float2ll_rn(va.z * 4294967296.0f);
+                    const float4 va = s_buf[o + q].vel;
+                    sx += fixed24(va.x);
+                    sy += fixed24(va.y);
+                    sz += fixed24(va.z);
                 }
                 sx += tx;
                 sy += ty;
@@ -853,12 +915,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                 sy = group_sum(sy, G);
                 sz = group_sum(sz, G);
                 if (in_sub && leader) {
-                    float3 mean = make_float3(0, 0, 0);
-                    if (n > 1) {
-                        const float inv = 1.0f / (float)n;
-                        mean = make_float3((__ll2float_rn(sx) * 0x1p-32f) * inv, (__ll2float_rn(sy) * 0x1p-32f) * inv,
-                                           (__ll2float_rn(sz) * 0x1p-32f) * inv);
-                    }
+                    const float3 mean = n > 1 ? srd_mean(sx, sy, sz, n) : make_float3(0, 0, 0);
                     L.c0[i] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(n));   // axis: c1, drawn per tile
                     if (!REPLAY && a.tape_ncell) a.tape_ncell[b.cell_base + c0 + i] = n > 1 ? n : 0u;
                 }
@@ -891,7 +948,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                 float real_vz = 0.0f;
                 for (uint32_t k = my_j; ext_lane && live && k < n; k += kExtLanes) {
                     const uint32_t p = at(k);
-                    const float4 xp = s_pos[p], vp = s_vel[p];
+                    const float4 xp = s_buf[p].pos, vp = s_buf[p].vel;
                     com.x += (xp.x - centre.x); com.y += (xp.y - centre.y); com.z += (xp.z - centre.z);
                     mean.x += vp.x; mean.y += vp.y; mean.z += vp.z;
                     if (k < m) real_vz += vp.z;
@@ -908,11 +965,11 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                 int size0 = 0;
                 for (uint32_t k = my_j; ext_lane && live && k < n; k += kExtLanes) {
                     const uint32_t p = at(k);
-                    float4 xp = s_pos[p], vp = s_vel[p];
+                    float4 xp = s_buf[p].pos, vp = s_buf[p].vel;
                     xp.x -= com.x; xp.y -= com.y; xp.z -= com.z;
                     vp.x -= mean.x; vp.y -= mean.y; vp.z -= mean.z;
-                    s_pos[p] = xp;
-                    s_vel[p] = vp;
+                    s_buf[p].pos = xp;
+                    s_buf[p].vel = vp;
                     if (dot3(make_float3(xp.x, xp.y, xp.z), axis) < 0) {
                         proj0 += dot3(make_float3(vp.x, vp.y, vp.z), axis);
                         size0 += 1;
@@ -954,8 +1011,8 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                     }
                     if (k >= n) continue;
                     const uint32_t p = at(k);
-                    const float4 xp = s_pos[p];
-                    float4 vp = s_vel[p];
+                    const float4 xp = s_buf[p].pos;
+                    float4 vp = s_buf[p].vel;
                     const float3 x = make_float3(xp.x, xp.y, xp.z);
                     float3 v = make_float3(vp.x, vp.y, vp.z);
                     const bool sd = dot3(x, axis) < 0;
@@ -965,7 +1022,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                     dL.x += cr.x; dL.y += cr.y; dL.z += cr.z;
                     const float kick = (vr - dot3(v, axis)) + (sd ? t0 : t1);
                     v.x += axis.x * kick; v.y += axis.y * kick; v.z += axis.z * kick;
-                    s_vel[p] = make_float4(v.x, v.y, v.z, vp.w);
+                    s_buf[p].vel = make_float4(v.x, v.y, v.z, vp.w);
                     const float sx = x.x * x.x, sy = x.y * x.y, sz = x.z * x.z;
                     I[0] += sy + sz;
                     I[1] += sx + sz;
@@ -983,12 +1040,12 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                 const float3 vm1 = make_float3(axis.x * m1, axis.y * m1, axis.z * m1);
                 for (uint32_t k = my_j; ext_lane && collide && k < n; k += kExtLanes) {
                     const uint32_t p = at(k);
-                    const float4 xp = s_pos[p];
-                    float4 vp = s_vel[p];
+                    const float4 xp = s_buf[p].pos;
+                    float4 vp = s_buf[p].vel;
                     const float3 x = make_float3(xp.x, xp.y, xp.z);
                     const float3 vm = dot3(x, axis) < 0 ? vm0 : vm1;
                     vp.x -= vm.x; vp.y -= vm.y; vp.z -= vm.z;
-                    s_vel[p] = vp;
+                    s_buf[p].vel = vp;
                     const float3 cr = cross3(x, make_float3(vp.x, vp.y, vp.z));
                     dL.x -= cr.x; dL.y -= cr.y; dL.z -= cr.z;
                 }
@@ -1014,7 +1071,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                 if (p >= np) continue;
                 const uint32_t info = s_cell[p];
                 const uint32_t ci = info & ~kGhostFlag;
-                if (info & kGhostFlag) reinterpret_cast<uint32_t*>(s_pos + p)[3] = kNoKey;
+                if (info & kGhostFlag) s_buf[p].pos.w = __uint_as_float(kNoKey);
                 else finish(p, ci, L.c0[ci], L.c1[ci]);
             }
             if (REPLAY) {
@@ -1037,7 +1094,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                     base[j] = 0;
                     if (j >= jmax) continue;
                     const uint32_t p = (uint32_t)tid + (uint32_t)kThreads * j;
-                    key[j] = p < np ? __float_as_uint(s_pos[p].w) : kNoKey;
+                    key[j] = p < np ? __float_as_uint(s_buf[p].pos.w) : kNoKey;
                     const bool act = key[j] != kNoKey;
                     const unsigned m = __ballot_sync(kFull, act);
                     peers[j] = 0;
@@ -1053,12 +1110,10 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                     const uint32_t p = (uint32_t)tid + (uint32_t)kThreads * j;
                     const uint32_t slot =
                         __shfl_sync(peers[j], base[j], __ffs(peers[j]) - 1) + __popc(peers[j] & lanemask_lt());
-                    const float4 xs = s_pos[p], vp = s_vel[p];
+                    const float4 xs = s_buf[p].pos, vp = s_buf[p].vel;
                     const float4 xp = make_float4(xs.x, xs.y, xs.z, 0.0f);
                     if (slot < b.cap) {
-                        const uint64_t at = b.slot_base + (uint64_t)(key[j] - b.cell_base) * b.cap + slot;
-                        a.out_pos[at] = xp;
-                        a.out_vel[at] = vp;
+                        store_slot(a.out_slots + b.slot_base + (uint64_t)(key[j] - b.cell_base) * b.cap + slot, xp, vp);
                     } else {
                         push_overflow(a, key[j], xp, vp);
                     }
@@ -1078,6 +1133,217 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
     }
 }
 
+// ------------------------------------------------------------------ SRD run kernel
+//
+// The production SRD step of one box (Philox draws; replays, the adjoint tape
+// and the pressure estimator take step_kernel): one warp per run of 32
+// consecutive cells (storage order), lane l owning cell l of the run.  No
+// CTA-wide barrier and no staging: each warp works alone on its runs with 1.5
+// KB of shared memory of its own, and reads the particles straight from their
+// buckets (a cell's bucket is contiguous).  Per run:
+//   per cell (its lane): count, wall ghosts (drawn by the step's prologue),
+//   rotation axis;
+//   then batches of 8 cells: exact velocity sums of the batch's particles (4
+//   lanes per cell, four loads in flight each), and per particle, 32
+//   consecutive particles of the batch at a time (their slots still in L1 from
+//   the sums): the collision, unshift, drag, lab-grid sample, streaming of step
+//   k+1 and its cell, the slot claim (warp-aggregated) and one 256-bit store.
+//   Each batch asks L2 for the next batch's buckets.
+// The arithmetic is step_kernel's (the same helpers), so a replay of this step
+// by step_kernel (the getters) reproduces it bit for bit.
+
+constexpr uint32_t kRunCells = 32;
+constexpr uint32_t kBatchCells = 8;                   // cells summed and finished together
+constexpr uint32_t kBatchLanes = 32 / kBatchCells;    // lanes per cell in the sums
+constexpr int kRunWarps = kThreads / 32;
+constexpr uint32_t kRunMaxN = 64;                     // densities this kernel takes
+
+struct RunShared {                   // one per warp
+    float4 cell[kRunCells];          // mean velocity, entries (particles + ghosts) as bits
+    float4 axis[kRunCells];          // rotation axis
+    long long gsum[kRunCells][3];    // exact velocity sums of the cell's ghosts
+};
+
+// Bring `bytes` (a multiple of 16, 16-byte aligned) of global memory into L2.
+__device__ __forceinline__ void prefetch_l2(const void* src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
+// A whole slot with one 256-bit load (the buckets of step k are read-only here).
+__device__ __forceinline__ void load_slot(const Slot* src, float4& p, float4& v)
+{
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w), "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(src));
+}
+
+template <bool SAMPLE>
+__global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a)
+{
+    __shared__ RunShared shared_runs[kRunWarps];
+    const uint32_t lane = threadIdx.x & 31u;
+    RunShared& sh = shared_runs[threadIdx.x >> 5];
+    const BoxDesc& b = a.box0;
+    const uint64_t step = a.step_base ? *a.step_base + a.step : a.step;   // graph replays read the base
+
+    if (blockIdx.x == 0) {
+        if (threadIdx.x == 0) a.state->ov_count[a.ov_zero_slot] = 0;   // list of step k-1, refilled by step k+1
+        overflow_pass(a, step);
+    }
+    const float3 s = grid_shift(b, 0, step, a.state);
+    const float3 sn = grid_shift(b, 0, step + 1, a.state);
+    const bool sign = s.z > 0;
+    const uint32_t runs = (b.C + kRunCells - 1) / kRunCells;
+    const uint32_t warps = gridDim.x * (uint32_t)kRunWarps;
+    uint32_t run = blockIdx.x * (uint32_t)kRunWarps + (threadIdx.x >> 5);
+    uint32_t raw_next = 0;   // the count of this lane's cell, fetched one run ahead
+    if (run < runs && run * kRunCells + lane < b.C) raw_next = a.in_count[b.cell_base + run * kRunCells + lane];
+    if (lane < kBatchCells && raw_next)   // the first batch of the first run
+        prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(run * kRunCells + lane) * b.cap,
+                    min(raw_next, b.cap) * (uint32_t)sizeof(Slot));
+
+    for (; run < runs; run += warps) {
+        const uint32_t c = run * kRunCells + lane;
+        const bool valid = c < b.C;
+        const uint32_t cnt = min(raw_next, b.cap);
+        if (valid) a.zero_count[b.cell_base + c] = 0;   // counts of step k-1: step k+1 fills them
+        {
+            const uint32_t cn = c + warps * kRunCells;
+            raw_next = (run + warps < runs && cn < b.C) ? a.in_count[b.cell_base + cn] : 0u;
+        }
+        const Slot* const bucket0 = a.in_slots + b.slot_base + (uint64_t)run * kRunCells * b.cap;
+        const uint3 cc = storage_coords(b, valid ? c : 0u);
+        bool layer, wall;
+        wall_layer(b, cc.z, sign, layer, wall);
+        wall = wall && valid;
+        // wall ghosts (drawn by the step's prologue): count and exact velocity sums
+        uint32_t ng = 0;
+        {
+            long long gx = 0, gy = 0, gz = 0;
+            if (wall) {
+                const GhostSum& g =
+                    a.ghosts[b.wall_base + 2u * (cc.x + (uint32_t)b.L[0] * cc.y) + (cc.z == (uint32_t)sign ? 0u : 1u)];
+                ng = g.n;
+                gx = g.sx;
+                gy = g.sy;
+                gz = g.sz;
+            }
+            sh.gsum[lane][0] = gx;
+            sh.gsum[lane][1] = gy;
+            sh.gsum[lane][2] = gz;
+        }
+        const uint32_t m = cnt + ng;   // entries of the cell's collision
+        if (m > 1) {
+            const float3 ax = srd_axis_philox(b, step, ref_index(b, cc));
+            sh.axis[lane] = make_float4(ax.x, ax.y, ax.z, 0.0f);
+        }
+        __syncwarp();
+
+        for (uint32_t c8 = 0; c8 < kRunCells; c8 += kBatchCells) {
+            // L2 prefetch of the next batch's buckets (after the last batch: the next run's first)
+            if (c8 + kBatchCells < kRunCells) {
+                if (lane >= c8 + kBatchCells && lane < c8 + 2 * kBatchCells && cnt)
+                    prefetch_l2(bucket0 + (uint64_t)lane * b.cap, cnt * (uint32_t)sizeof(Slot));
+            } else if (lane < kBatchCells && run + warps < runs && c + warps * kRunCells < b.C) {
+                const uint32_t nc = min(raw_next, b.cap);
+                if (nc)
+                    prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(c + warps * kRunCells) * b.cap,
+                                nc * (uint32_t)sizeof(Slot));
+            }
+            // exact sums of the batch's real particles: kBatchLanes lanes per cell
+            {
+                const uint32_t L = c8 + lane / kBatchLanes, jl = lane % kBatchLanes;
+                const uint32_t cntL = __shfl_sync(kFull, cnt, (int)L), mL = __shfl_sync(kFull, m, (int)L);
+                const Slot* src = bucket0 + (uint64_t)L * b.cap;
+                long long sx = 0, sy = 0, sz = 0;
+                unsigned mx = 0;
+                for (uint32_t j = jl; j < cntL; j += 4 * kBatchLanes) {   // four loads in flight per lane
+                    float4 v[4];
+#pragma unroll
+                    for (uint32_t u = 0; u < 4; ++u)
+                        v[u] = j + u * kBatchLanes < cntL ? __ldg(&src[j + u * kBatchLanes].vel) : make_float4(0, 0, 0, 0);
+                    int px = 0, py = 0, pz = 0;
+#pragma unroll
+                    for (uint32_t u = 0; u < 4; ++u) {
+                        px += fixed24_narrow(v[u].x, mx);
+                        py += fixed24_narrow(v[u].y, mx);
+                        pz += fixed24_narrow(v[u].z, mx);
+                    }
+                    sx += px;
+                    sy += py;
+                    sz += pz;
+                }
+                if (__any_sync(kFull, mx >= kNarrowLimit)) {   // a speed of 32 or more in the batch: 64-bit sums
+                    sx = sy = sz = 0;
+                    for (uint32_t j = jl; j < cntL; j += kBatchLanes) {
+                        const float4 v = __ldg(&src[j].vel);
+                        sx += fixed24(v.x);
+                        sy += fixed24(v.y);
+                        sz += fixed24(v.z);
+                    }
+                }
+#pragma unroll
+                for (uint32_t o = 1; o < kBatchLanes; o <<= 1) {
+                    sx += __shfl_xor_sync(kFull, sx, (int)o);
+                    sy += __shfl_xor_sync(kFull, sy, (int)o);
+                    sz += __shfl_xor_sync(kFull, sz, (int)o);
+                }
+                if (jl == 0) {
+                    sx += sh.gsum[L][0];
+                    sy += sh.gsum[L][1];
+                    sz += sh.gsum[L][2];
+                    const float3 mean = mL > 1 ? srd_mean(sx, sy, sz, mL) : make_float3(0, 0, 0);
+                    sh.cell[L] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(mL));
+                }
+            }
+            // the batch's particles in order, 32 at a time: particle t lies in batch
+            // cell i when end_{i-1} <= t < end_i (ends: inclusive prefix of the counts,
+            // held by lanes 0..7)
+            const uint32_t bc = __shfl_sync(kFull, cnt, (int)(c8 + (lane & (kBatchCells - 1))));
+            uint32_t bi = lane < kBatchCells ? bc : 0u;
+#pragma unroll
+            for (int d = 1; d < (int)kBatchCells; d <<= 1) {
+                const uint32_t t = __shfl_up_sync(kFull, bi, d);
+                if ((int)lane >= d) bi += t;
+            }
+            static_assert(kBatchCells == 8, "the search below covers 8 cells");
+            const uint32_t btot = __shfl_sync(kFull, bi, kBatchCells - 1);
+            __syncwarp();   // the batch's means are written
+            for (uint32_t e0 = 0; e0 < btot; e0 += 32) {
+                const uint32_t t = e0 + lane;
+                const bool active = t < btot;
+                // batch cell i of particle t: the number of cells that end at or before t
+                // (binary search over the ends), and its first particle
+                uint32_t i = t >= __shfl_sync(kFull, bi, 3) ? 4u : 0u;
+                i += t >= __shfl_sync(kFull, bi, (int)i + 1) ? 2u : 0u;
+                i += t >= __shfl_sync(kFull, bi, (int)i) ? 1u : 0u;
+                const uint32_t off = __shfl_sync(kFull, bi, (int)(i + 7u) & 7) & (i ? ~0u : 0u);
+                uint32_t key = 0, id = 0;
+                float3 xn = make_float3(0, 0, 0), vn = xn;
+                if (active) {
+                    const uint32_t L = c8 + i;
+                    float4 xp, vp;
+                    load_slot(bucket0 + (uint64_t)L * b.cap + (t - off), xp, vp);
+                    const float4 cd = sh.cell[L];
+                    float3 x = make_float3(xp.x, xp.y, xp.z), v = make_float3(vp.x, vp.y, vp.z);
+                    if (__float_as_uint(cd.w) > 1) {
+                        const float4 ax = sh.axis[L];
+                        srd_collide(b, s, make_float3(cd.x, cd.y, cd.z), make_float3(ax.x, ax.y, ax.z), x, v);
+                    }
+                    vn = v;
+                    xn = stream_shift(b, x, vn, sn);
+                    key = b.cell_base + storage_index(b, cell_of_wrapped(b, xn));
+                    id = __float_as_uint(vp.w);
+                    if (SAMPLE) sample_add(a.samp, b.cell_base + storage_index(b, cell_of_wrapped(b, x)), v, true);
+                }
+                store_particle(a, b, xn, vn, id, key, active);
+            }
+        }
+        __syncwarp();   // the next run rewrites this warp's shared arrays
+    }
+}
+
 // Before step k: in every cell that received more particles than its bucket
 // holds (raw count > cap), keep the cap lowest ids in the bucket and move the
 // others to the overflow list, whatever order the claims of step k-1 arrived in:
@@ -1088,9 +1354,46 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
 // with the bucket's largest id.  Overflow is rare: without any, every thread
 // returns after one load.  Run on the inputs of step k, so a replay of step k
 // finds them already in order.
-__global__ void __launch_bounds__(kThreads) overflow_select_kernel(const StepArgs a, float4* in_pos, float4* in_vel,
-                                                                   float4* ov_pos, float4* ov_vel)
+__global__ void __launch_bounds__(kThreads) overflow_select_kernel(const StepArgs a, Slot* in_slots, float4* ov_pos,
+                                                                   float4* ov_vel)
 {
+    // Wall ghosts of step k for srd_run_kernel: one thread per wall cell (the two
+    // ghost layers of every column) draws the ghost count and the ghosts' summed
+    // velocity, as step_kernel draws them, and stores the count and the exact
+    // velocity sums.  Drawn here, every thread busy, instead of by a few lanes
+    // of each run.
+    if (a.ghosts && a.box0.wall_z) {
+        const BoxDesc& b = a.box0;
+        const uint64_t step = a.step_base ? *a.step_base + a.step : a.step;
+        const float3 s = grid_shift(b, 0, step, a.state);
+        const float shift_abs = fabsf(s.z);
+        const bool sign = s.z > 0;
+        const uint32_t Lx = (uint32_t)b.L[0], Lz = (uint32_t)b.L[2];
+        const uint32_t walls = 2u * Lx * (uint32_t)b.L[1];
+        for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < walls; w += gridDim.x * blockDim.x) {
+            const uint32_t col = w >> 1, y = fast_div(col, b.div_x), x = col - y * Lx;
+            const uint32_t cz = (w & 1u) ? Lz - (sign ? 1u : 2u) : (sign ? 1u : 0u);
+            bool layer, ghosts;
+            wall_layer(b, cz, sign, layer, ghosts);
+            const uint32_t ref = ref_index(b, make_uint3(x, y, cz));
+            uint32_t g = 0;
+            for (uint32_t chunk = 0; 4 * chunk < b.n; ++chunk) {
+                const uint4 o = draw(b, step, kGhostCount, ref, chunk);
+                const uint32_t u[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (4 * chunk + k < b.n && ((u01(u[k]) > shift_abs) ^ layer ^ sign)) ++g;
+            }
+            GhostSum r{0, 0, 0, g, 0u};
+            if (g) {
+                const float3 v = ghost_sum_velocity(b, step, ref, g);
+                r.sx = fixed24(v.x);
+                r.sy = fixed24(v.y);
+                r.sz = fixed24(v.z);
+            }
+            a.ghosts[b.wall_base + w] = r;
+        }
+    }
     const uint32_t n = min(a.state->ov_count[a.ov_in_slot], a.ov_cap);
     for (uint32_t e0 = blockIdx.x * blockDim.x + threadIdx.x; e0 < n; e0 += gridDim.x * blockDim.x) {
         const float4 p0 = ov_pos[e0];
@@ -1103,9 +1406,9 @@ __global__ void __launch_bounds__(kThreads) overflow_select_kernel(const StepArg
         uint32_t e = e0;
         for (uint32_t t = b.cap; t < raw && e < a.ov_cap; ++t) {
             const uint32_t before = a.ov_next_in[e];
-            uint32_t jmax = 0, idmax = __float_as_uint(in_vel[base].w);
+            uint32_t jmax = 0, idmax = __float_as_uint(in_slots[base].vel.w);
             for (uint32_t j = 1; j < b.cap; ++j) {
-                const uint32_t id = __float_as_uint(in_vel[base + j].w);
+                const uint32_t id = __float_as_uint(in_slots[base + j].vel.w);
                 if (id > idmax) {
                     idmax = id;
                     jmax = j;
@@ -1113,10 +1416,10 @@ __global__ void __launch_bounds__(kThreads) overflow_select_kernel(const StepArg
             }
             const float4 pe = ov_pos[e], we = ov_vel[e];
             if (__float_as_uint(we.w) < idmax) {
-                ov_pos[e] = in_pos[base + jmax];
-                ov_vel[e] = in_vel[base + jmax];
-                in_pos[base + jmax] = pe;
-                in_vel[base + jmax] = we;
+                ov_pos[e] = in_slots[base + jmax].pos;
+                ov_vel[e] = in_slots[base + jmax].vel;
+                in_slots[base + jmax].pos = pe;
+                in_slots[base + jmax].vel = we;
             }
             e = before;
         }
@@ -1280,7 +1583,7 @@ __global__ void __launch_bounds__(kThreads) scan_kernel(const uint32_t* count, c
 // Layout dump: the particles of every cell, in stable order, cells in storage
 // order, followed by the overflow list.  offsets from scan_kernel.
 __global__ void __launch_bounds__(kThreads) compact_kernel(const StepArgs a, const uint32_t* count,
-                                                           const float4* pos, const float4* vel,
+                                                           const Slot* slots,
                                                            const uint32_t* offsets, uint64_t cells, uint64_t n_total,
                                                            uint32_t* out_cell, uint32_t* out_slot, uint32_t* out_prev,
                                                            uint32_t* out_id)
@@ -1298,10 +1601,10 @@ __global__ void __launch_bounds__(kThreads) compact_kernel(const StepArgs a, con
         const uint32_t dst0 = offsets[c];
         const uint32_t ref = ref_index(b, storage_coords(b, (uint32_t)(c - b.cell_base)));
         for (uint32_t q = 0; q < n; ++q) {
-            const uint32_t key = __float_as_uint(vel[slot0 + q].w);   // particle id
+            const uint32_t key = __float_as_uint(slots[slot0 + q].vel.w);   // particle id
             uint32_t rank = 0;
             for (uint32_t u = 0; u < n; ++u) {
-                const uint32_t ku = __float_as_uint(vel[slot0 + u].w);
+                const uint32_t ku = __float_as_uint(slots[slot0 + u].vel.w);
                 rank += ku < key || (ku == key && u < q);
             }
             const uint64_t d = (uint64_t)dst0 + rank;
@@ -1312,7 +1615,7 @@ __global__ void __launch_bounds__(kThreads) compact_kernel(const StepArgs a, con
             if (out_cell) out_cell[d] = b.cell_base + ref;
             if (out_slot) out_slot[d] = (uint32_t)(slot0 + rank);
             if (out_prev) out_prev[d] = key;
-            if (out_id) out_id[d] = __float_as_uint(vel[slot0 + q].w);
+            if (out_id) out_id[d] = __float_as_uint(slots[slot0 + q].vel.w);
         }
     }
 }
@@ -1524,8 +1827,19 @@ const StepFn kStepFns[2][2][2][2] = {
       {step_kernel<1, true, true, false>, step_kernel<1, true, true, true>}}}};
 }  // namespace
 
+bool run_kernel_takes(const StepArgs& a, int algorithm, bool table)
+{
+    return algorithm == 0 && !table && a.nboxes == 1 && !a.replay && !a.tape_key && !a.pressure &&
+           a.box0.n <= kRunMaxN && (a.ghosts || !a.box0.wall_z);
+}
+
 cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st)
 {
+    if (run_kernel_takes(a, algorithm, table)) {
+        if (a.sample) srd_run_kernel<true><<<grid, kThreads, 0, st>>>(a);
+        else srd_run_kernel<false><<<grid, kThreads, 0, st>>>(a);
+        return cudaGetLastError();
+    }
     const size_t smem = step_smem_bytes(pbuf, a.boxes_tile_cells, algorithm);
     kStepFns[algorithm ? 1 : 0][table ? 1 : 0][a.nboxes == 1 ? 1 : 0][a.replay ? 1 : 0]<<<grid, kThreads, smem, st>>>(
         a, pbuf);
@@ -1564,6 +1878,10 @@ cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* bl
     // load the kernels that step graphs capture before any capture begins
     cudaFuncAttributes attr;
     e = cudaFuncGetAttributes(&attr, (const void*)advance_kernel);
+    // the run kernel: about a quarter of the unified array as shared memory (4
+    // CTAs of 14 KB), the rest L1, which holds each batch's slots between its two passes
+    for (const void* f : {(const void*)srd_run_kernel<false>, (const void*)srd_run_kernel<true>})
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 27);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, (const void*)sample_finalize_kernel);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, (const void*)overflow_select_kernel);
     if (e != cudaSuccess) return e;
@@ -1610,10 +1928,10 @@ cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel
     return cudaGetLastError();
 }
 
-cudaError_t launch_overflow_select(const StepArgs& a, float4* in_pos, float4* in_vel, float4* ov_pos, float4* ov_vel,
-                                   int grid, cudaStream_t st)
+cudaError_t launch_overflow_select(const StepArgs& a, Slot* in_slots, float4* ov_pos, float4* ov_vel, int grid,
+                                   cudaStream_t st)
 {
-    overflow_select_kernel<<<grid, kThreads, 0, st>>>(a, in_pos, in_vel, ov_pos, ov_vel);
+    overflow_select_kernel<<<grid, kThreads, 0, st>>>(a, in_slots, ov_pos, ov_vel);
     return cudaGetLastError();
 }
 
@@ -1632,7 +1950,7 @@ cudaError_t launch_mean_fields(const SampleAcc* acc, const BoxDesc& b, double in
     return cudaGetLastError();
 }
 
-cudaError_t launch_layout(const StepArgs& a, const uint32_t* count, const float4* pos, const float4* vel,
+cudaError_t launch_layout(const StepArgs& a, const uint32_t* count, const Slot* slots,
                           uint32_t* offsets, uint64_t cells, uint64_t n_total, unsigned long long* status,
                           unsigned int* tile_counter, const float4* ov_pos, const float4* ov_vel, unsigned parity,
                           uint32_t* out_cell, uint32_t* out_slot, uint32_t* out_prev, uint32_t* out_id, int grid,
@@ -1645,7 +1963,7 @@ cudaError_t launch_layout(const StepArgs& a, const uint32_t* count, const float4
     if (e != cudaSuccess) return e;
     scan_kernel<<<(unsigned)tiles, kThreads, 0, st>>>(count, a.boxes, a.nboxes, cells, offsets, status, tile_counter,
                                                       a.state);
-    compact_kernel<<<grid, kThreads, 0, st>>>(a, count, pos, vel, offsets, cells, n_total, out_cell, out_slot,
+    compact_kernel<<<grid, kThreads, 0, st>>>(a, count, slots, offsets, cells, n_total, out_cell, out_slot,
                                               out_prev, out_id);
     compact_overflow_kernel<<<8, kThreads, 0, st>>>(a.boxes, a.nboxes, a.step, ov_pos, ov_vel, a.state, parity,
                                                     a.ov_cap, offsets, cells, n_total, a.total_slots, out_cell,

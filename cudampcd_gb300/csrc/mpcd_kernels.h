@@ -16,6 +16,10 @@ size_t step_smem_bytes(uint32_t pbuf, uint32_t cells, int algorithm);
 cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* blocks_per_sm);
 // One step of every box (algorithm 0 = SRD, 1 = extended; table = injected draws).
 cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st);
+// Whether launch_step runs this step with srd_run_kernel (SRD, one box, Philox
+// draws, no replay, tape or pressure estimator, n <= 64, and the wall ghosts of
+// the step drawn by its prologue when the box has walls).
+bool run_kernel_takes(const StepArgs& a, int algorithm, bool table);
 // state->step_base += steps (the last node of a replayed step graph).
 cudaError_t launch_advance(DeviceState* state, unsigned steps, cudaStream_t st);
 // Key dense clean particles for step a.step + 1 and scatter them into a.out_*.
@@ -24,7 +28,7 @@ cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel
 // Before a step (not a replay): the particles the reference keeps in each overflowing
 // cell into its bucket, the others into the overflow list (in_* / ov_*: the step's
 // input buckets and list, a.in_count, a.ov_head_in and a.ov_next_in its chains).
-cudaError_t launch_overflow_select(const StepArgs& a, float4* in_pos, float4* in_vel, float4* ov_pos, float4* ov_vel,
+cudaError_t launch_overflow_select(const StepArgs& a, Slot* in_slots, float4* ov_pos, float4* ov_vel,
                                    int grid, cudaStream_t st);
 // Lab-grid sample of one step into the FP64 running sums (and clear the step sums).
 cudaError_t launch_sample_finalize(float4* samp, SampleAcc* acc, uint64_t cells, int snapshot, int grid,
@@ -45,7 +49,7 @@ cudaError_t launch_adjoint_finish(uint32_t n, const float* lam, const uint32_t* 
 // Layout dump: cells in storage order, stable order within a cell (decoupled
 // look-back scan of the counts, then one thread per cell), then the overflow
 // list.  offsets: cells + 1 entries.
-cudaError_t launch_layout(const StepArgs& a, const uint32_t* count, const float4* pos, const float4* vel,
+cudaError_t launch_layout(const StepArgs& a, const uint32_t* count, const Slot* slots,
                           uint32_t* offsets, uint64_t cells, uint64_t n_total, unsigned long long* status,
                           unsigned int* tile_counter, const float4* ov_pos, const float4* ov_vel, unsigned parity,
                           uint32_t* out_cell, uint32_t* out_slot, uint32_t* out_prev, uint32_t* out_id, int grid,

@@ -1,8 +1,8 @@
 // Host/device data structures of the GB300 MPCD step.
 //
 // Particles live in per-cell buckets: cell c of a box owns `cap` slots
-// (cap = 4n, the depth of the reference's cell table, backend_context.cu:24),
-// stored as two float4 arrays: pos = (x, y, z, 0) and vel = (vx, vy, vz, id).
+// (cap = 4n, the depth of the reference's cell table, backend_context.cu:24) of
+// 32 bytes each, one DRAM sector: pos = (x, y, z, 0), vel = (vx, vy, vz, id).
 // A bucket set for step k holds every particle as it enters the collision of
 // step k: streamed and shifted by the grid shift of step k, in the bucket of the
 // cell it then occupies (the reference's translate output, simulation_functions.cpp:38-103).
@@ -14,8 +14,17 @@
 #pragma once
 
 #include <cstdint>
+#include <vector_types.h>
 
 namespace mpcd_gb {
+
+// One bucket slot: a particle's position and velocity with its id in vel.w (the
+// bit pattern of a float), 32 bytes, so that a particle is one full sector in
+// DRAM and one 256-bit access.
+struct alignas(32) Slot {
+    float4 pos;
+    float4 vel;
+};
 
 constexpr int kThreads = 256;        // threads per CTA of the step kernel
 constexpr int kMaxInjectedShifts = 4;
@@ -45,6 +54,8 @@ struct BoxDesc {
     uint64_t dense_base;   // first particle of this box in dense (getter) arrays
     uint64_t div_z, div_x; // ceil(2^48 / Lz), ceil(2^48 / Lx): exact division of cell indices < 2^31
     uint32_t seed_lo, seed_hi;
+    uint64_t wall_base;    // first wall-ghost entry of this box (2 per column, with walls in z)
+    uint64_t unused;
 };
 
 // The step kernel copies a box descriptor into shared memory 16 bytes per thread.
@@ -55,6 +66,14 @@ struct alignas(16) TileEntry {
     uint32_t first;   // first global cell (storage order)
     uint32_t cells;   // cells of this tile | cells per tile of its box << 16
     uint32_t box;
+    uint32_t unused;
+};
+
+// The wall ghosts of one wall cell for one step (srd_run_kernel): their count
+// and the exact sum of their velocities (multiples of 2^-24).
+struct alignas(32) GhostSum {
+    long long sx, sy, sz;
+    uint32_t n;
     uint32_t unused;
 };
 
@@ -104,12 +123,10 @@ struct StepArgs {
     uint64_t step;                // k: this launch completes step k (step_base: k - *step_base)
     const unsigned long long* step_base;   // non-null in graph replays: k = *step_base + step
     // buckets holding the particles entering collision k (streamed, shifted)
-    const float4* in_pos;
-    const float4* in_vel;
+    const Slot* in_slots;
     const uint32_t* in_count;
     // buckets receiving the particles entering collision k+1
-    float4* out_pos;
-    float4* out_vel;
+    Slot* out_slots;
     uint32_t* out_count;
     uint32_t* zero_count;         // counts of step k-1: cleared here for step k+1
     // overflow lists: in = pending for step k, out = for step k+1
@@ -152,6 +169,9 @@ struct StepArgs {
     // pressure estimator on: accumulate the z impulse the fluid gives the walls
     // (bounce-backs and collisions in the wall-layer cells) into state->wall_impulse
     int32_t pressure;
+    // srd_run_kernel steps: the wall ghosts of step k, drawn by the step's
+    // prologue (overflow_select_kernel), entry wall_base + 2 (x + Lx y) + top
+    GhostSum* ghosts;
 };
 
 constexpr uint32_t kTapeNone = 0xFFFFFFFFu;

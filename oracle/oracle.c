@@ -131,7 +131,7 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 
 /* Draw model of the GPU backend.  Counter = {a, step_lo, purpose | step_hi << 8, d},
  * key = seed.  Purposes: */
-enum { GB_SHIFT = 1, GB_AXIS = 2, GB_GHOST_COUNT = 3, GB_GHOST = 4, GB_THERMAL = 5 };
+enum { GB_SHIFT = 1, GB_AXIS = 2, GB_GHOST_COUNT = 3, GB_GHOST = 4, GB_THERMAL = 5, GB_GHOST_SUM = 7 };
 
 static void gb_draw(uint64_t seed, uint64_t step, uint32_t purpose, uint32_t a, uint32_t d, uint32_t out[4])
 {
@@ -549,7 +549,29 @@ int orc_srd_collision(const orc_params *p, float *pos, float *vel, uint32_t *cel
             memcpy(buf[i].x, pos + 3 * (size_t)k, sizeof buf[i].x);
             memcpy(buf[i].v, vel + 3 * (size_t)k, sizeof buf[i].v);
         }
-        if (add_ghosts) {
+        if (add_ghosts && d->mode == ORC_DRAWS_PHILOX) {
+            /* The GPU's draw model of SRD ghosts: their summed velocity, one
+             * Gaussian of variance g T per component, carried by the first ghost
+             * (the SRD collision uses the ghosts only through their sum). */
+            float centre[3];
+            cell_centre(p, c, centre);
+            for (uint32_t i = n - g; i < n; ++i) {
+                memcpy(buf[i].x, centre, sizeof buf[i].x);
+                buf[i].v[0] = buf[i].v[1] = buf[i].v[2] = 0.0f;
+                buf[i].idx = -1;
+            }
+            if (g) {
+                uint32_t o[4];
+                gb_draw(d->seed, d->step, GB_GHOST_SUM, c, 0, o);
+                float g0, g1, g2, g3;
+                gb_box_muller(o[0], o[1], &g0, &g1);
+                gb_box_muller(o[2], o[3], &g2, &g3);
+                float sc = sqrtf((float)g) * p->thermal_velocity;
+                buf[n - g].v[0] = g0 * sc;
+                buf[n - g].v[1] = g1 * sc;
+                buf[n - g].v[2] = g2 * sc;
+            }
+        } else if (add_ghosts) {
             float centre[3];
             cell_centre(p, c, centre);
             for (uint32_t i = n - g; i < n; ++i)
