@@ -1153,8 +1153,10 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
 // by step_kernel (the getters) reproduces it bit for bit.
 
 constexpr uint32_t kRunCells = 32;
-constexpr uint32_t kBatchCells = 8;                   // cells summed and finished together
+constexpr uint32_t kBatchCells = 4;                   // cells summed and finished together
 constexpr uint32_t kBatchLanes = 32 / kBatchCells;    // lanes per cell in the sums
+static_assert(kBatchCells >= 2 && kBatchCells <= 16 && (kBatchCells & (kBatchCells - 1)) == 0,
+              "batches of a power of two of cells, searched by halving");
 constexpr int kRunWarps = kThreads / 32;
 constexpr uint32_t kRunMaxN = 64;                     // densities this kernel takes
 
@@ -1307,7 +1309,6 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a)
                 const uint32_t t = __shfl_up_sync(kFull, bi, d);
                 if ((int)lane >= d) bi += t;
             }
-            static_assert(kBatchCells == 8, "the search below covers 8 cells");
             const uint32_t btot = __shfl_sync(kFull, bi, kBatchCells - 1);
             __syncwarp();   // the batch's means are written
             for (uint32_t e0 = 0; e0 < btot; e0 += 32) {
@@ -1315,10 +1316,11 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a)
                 const bool active = t < btot;
                 // batch cell i of particle t: the number of cells that end at or before t
                 // (binary search over the ends), and its first particle
-                uint32_t i = t >= __shfl_sync(kFull, bi, 3) ? 4u : 0u;
-                i += t >= __shfl_sync(kFull, bi, (int)i + 1) ? 2u : 0u;
-                i += t >= __shfl_sync(kFull, bi, (int)i) ? 1u : 0u;
-                const uint32_t off = __shfl_sync(kFull, bi, (int)(i + 7u) & 7) & (i ? ~0u : 0u);
+                uint32_t i = 0;
+#pragma unroll
+                for (uint32_t half = kBatchCells / 2; half; half >>= 1)
+                    i += t >= __shfl_sync(kFull, bi, (int)(i + half - 1)) ? half : 0u;
+                const uint32_t off = __shfl_sync(kFull, bi, (int)((i + kBatchCells - 1) & (kBatchCells - 1))) & (i ? ~0u : 0u);
                 uint32_t key = 0, id = 0;
                 float3 xn = make_float3(0, 0, 0), vn = xn;
                 if (active) {

@@ -64,9 +64,17 @@ def oracle_blocks(alg, L, n, steps, blocks, seed):
 
 
 def test_srd_wall_pressure_is_the_ideal_gas_pressure():
+    """Three independent runs; the error bar comes from their spread.  Consecutive
+    blocks of one run are correlated (the pressure relaxes slowly), and their
+    standard error understates the spread of independent runs by a factor of about
+    three (eight seeds: block z-scores up to 4.6, seed means within 0.3 % of n T)."""
     n, T = 10, 1.3
-    P, err, layers = gpu_blocks(0, (16, 16, 22), n, 2000, 10, seed=4, T=T)
-    print(f"SRD wall pressure {P:.4f} +- {err:.4f}, n T = {n * T}")
+    runs = [gpu_blocks(0, (16, 16, 22), n, 2000, 10, seed=seed, T=T) for seed in (4, 5, 6)]
+    means = np.array([r[0] for r in runs])
+    P = means.mean()
+    err = max(means.std(ddof=1) / np.sqrt(len(means)), max(r[1] for r in runs))
+    layers = np.mean([r[2] for r in runs], axis=0)
+    print(f"SRD wall pressure {P:.4f} +- {err:.4f} (runs {means}), n T = {n * T}")
     assert abs(P - n * T) < max(4 * err, 1e-3 * n * T)
     assert abs(P / (n * T) - 1) < 0.01
     fluid = layers[1:-1]
