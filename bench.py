@@ -147,7 +147,7 @@ class ClockSampler:
 
 def ncu_traffic_per_particle():
     """DRAM bytes per particle of the step kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "step_kernel_traffic.json")
+    path = os.path.join(ROOT, "profiles", "srd_run_kernel_traffic.json")
     try:
         with open(path) as f:
             d = json.load(f)
@@ -496,7 +496,7 @@ def run_gpu_arm(args, rank, world, local_rank):
         peak, peak_kind = peaks()
         per_launch_ms = kernel_ms / args.steps
         achieved = ALGO_BYTES_PER_PARTICLE * N / (per_launch_ms * 1e-3) / 1e9
-        bpp, src = ncu_traffic_per_particle()
+        bpp, src = ncu_traffic_per_particle() if algorithm == 0 else (None, None)
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed / args.steps, "higher_is_better": True,
@@ -510,7 +510,8 @@ def run_gpu_arm(args, rank, world, local_rank):
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": bpp * N if bpp else None, "traffic_source": src,
                          "algorithmic_bytes_per_particle": ALGO_BYTES_PER_PARTICLE,
-                         "kernel": f"step_kernel<{args.algorithm.upper()}, Philox>", "kernel_ms": per_launch_ms},
+                         "kernel": "srd_run_kernel" if algorithm == 0 else "step_kernel<EXTENDED, Philox>",
+                         "kernel_ms": per_launch_ms},
             "e2e": e2e,
             "clocks": clocks.summary(),
             "gpu_launches": 2 * args.steps,   # per step: overflow selection, step kernel
