@@ -823,6 +823,7 @@ private:
         N_ = particles;
         cells_ = cells;
         walls_ = walls;
+        n_max_ = n_max;
         total_slots_ = slots;
         ov_cap_ = (uint32_t)std::max<uint64_t>(1u << 16, std::min<uint64_t>(N_, 1u << 22));
         if (total_slots_ + ov_cap_ >= (1ull << 32))
@@ -897,6 +898,13 @@ private:
                 tile_info_.push_back({b.cell_base + t * tc, std::min(tc, b.C - t * tc) | (tc << 16), (uint32_t)r, 0u});
         }
         tiles_ = tiles;
+        // runs of up to 32 cells of one box (srd_run_kernel): {first cell, cells | box << 6}
+        run_info_.clear();
+        for (size_t r = 0; r < boxes_.size(); ++r) {
+            const BoxDesc& b = boxes_[r];
+            for (uint32_t c = 0; c < b.C; c += 32)
+                run_info_.push_back(make_uint2(b.cell_base + c, std::min(32u, b.C - c) | ((uint32_t)r << 6)));
+        }
         pbuf_ = pbuf;
         fill_ = fill;
         for (auto& g : graph_) g.reset();   // graphs bake the tiling into their launches
@@ -918,6 +926,9 @@ private:
         const size_t bytes = sizeof(TileEntry) * tile_info_.size();
         if (tile_info_d_.bytes < bytes) check(tile_info_d_.alloc(bytes), "alloc tile table");
         check(cudaMemcpy(tile_info_d_.p, tile_info_.data(), bytes, cudaMemcpyHostToDevice), "upload tile table");
+        const size_t rbytes = sizeof(uint2) * run_info_.size();
+        if (run_info_d_.bytes < rbytes) check(run_info_d_.alloc(rbytes), "alloc run table");
+        check(cudaMemcpy(run_info_d_.p, run_info_.data(), rbytes, cudaMemcpyHostToDevice), "upload run table");
     }
 
     void allocate()
@@ -936,6 +947,7 @@ private:
             check(cudaMemset(count_[k].p, 0, count_[k].bytes), "clear counts");
         }
         if (walls_) check(ghosts_.alloc(sizeof(GhostSum) * walls_), "alloc wall ghosts");
+        if (boxes_.size() > 1) check(box_shifts_.alloc(sizeof(float4) * 2 * boxes_.size()), "alloc box shifts");
         check(state_.alloc(sizeof(DeviceState)), "alloc state");
         check(cudaMemset(state_.p, 0, sizeof(DeviceState)), "clear state");
         check(samp_.alloc(sizeof(float4) * cells_), "alloc sample");
@@ -1001,6 +1013,12 @@ private:
         a.boxes_tile_cells = max_tile_cells_;
         a.num_tiles = (uint32_t)tiles_;
         a.tile_info = tile_info_d_.as<TileEntry>();
+        a.run_info = boxes_.size() > 1 ? run_info_d_.as<uint2>() : nullptr;
+        a.num_runs = (uint32_t)run_info_.size();
+        a.boxes_n_max = n_max_;
+        a.total_walls = walls_;
+        a.ghosts = ghosts_.as<GhostSum>();
+        a.box_shifts = boxes_.size() > 1 ? box_shifts_.as<float4>() : nullptr;
         a.total_slots = total_slots_;
         a.step = k;
         const unsigned p = (unsigned)(k & 1), q = p ^ 1u;
@@ -1108,15 +1126,14 @@ private:
     {
         const unsigned p = (unsigned)(k & 1);
         return launch_overflow_select(a, slots_[p].as<Slot>(), ov_pos_[p].as<float4>(), ov_vel_[p].as<float4>(),
-                                      a.ghosts ? sms_ * 8 : sms_, st);
+                                      a.run_kernel && (a.total_walls || a.box_shifts) ? sms_ * 8 : sms_, st);
     }
 
     // The wall-ghost array of srd_run_kernel for a step that it runs (its prologue
     // draws the ghosts), else none.
     void use_run_kernel_ghosts(StepArgs& a, bool table) const
     {
-        a.ghosts = ghosts_.as<GhostSum>();
-        if (!run_kernel_takes(a, params_.algorithm, table)) a.ghosts = nullptr;
+        a.run_kernel = run_kernel_takes(a, params_.algorithm, table) ? 1 : 0;
     }
 
     // One step: the overflow selection, then the step kernel (bracketed by the
@@ -1297,8 +1314,11 @@ private:
     float inject_shift_[kMaxInjectedShifts][3] = {};
     std::vector<TileEntry> tile_info_;   // tile table of the current tiling
     DeviceBuffer tile_info_d_;
+    std::vector<uint2> run_info_;        // run table of srd_run_kernel
+    DeviceBuffer run_info_d_;
+    uint32_t n_max_ = 0;
     DeviceBuffer ov_head_[2], ov_next_[2];   // overflow chains: heads by cell, links by entry (by step parity)
-    DeviceBuffer boxes_d_, slots_[2], ghosts_, count_[3], ov_pos_[2], ov_vel_[2], state_, samp_, acc_, dense_pos_,
+    DeviceBuffer boxes_d_, slots_[2], ghosts_, box_shifts_, count_[3], ov_pos_[2], ov_vel_[2], state_, samp_, acc_, dense_pos_,
         dense_vel_, offsets_, scan_status_, scan_counter_, partial_;
     DeviceBuffer t_count_, t_gpos_, t_gvel_, t_axis_, t_gate_, t_gauss_;
     // adjoint: checkpoints, tape of one segment, adjoint state

@@ -1180,41 +1180,66 @@ __device__ __forceinline__ void load_slot(const Slot* src, float4& p, float4& v)
         : "l"(src));
 }
 
-template <bool SAMPLE>
+// Run `run` of the launch: {first global cell, cells | box << 6}.
+template <bool SINGLE>
+__device__ __forceinline__ uint2 run_entry(const StepArgs& a, uint32_t run)
+{
+    if (run >= a.num_runs) return make_uint2(0u, 0u);
+    if (!SINGLE) return __ldg(a.run_info + run);
+    const uint32_t c0 = run * kRunCells;
+    return make_uint2(a.box0.cell_base + c0, min(kRunCells, a.box0.C - c0));
+}
+
+template <bool SAMPLE, bool SINGLE>
 __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a)
 {
     __shared__ RunShared shared_runs[kRunWarps];
+    __shared__ __align__(16) BoxDesc shared_box[SINGLE ? 1 : kRunWarps];   // ensembles: the box of the warp's run
     const uint32_t lane = threadIdx.x & 31u;
     RunShared& sh = shared_runs[threadIdx.x >> 5];
-    const BoxDesc& b = a.box0;
+    BoxDesc& sbox = shared_box[SINGLE ? 0 : threadIdx.x >> 5];
     const uint64_t step = a.step_base ? *a.step_base + a.step : a.step;   // graph replays read the base
 
     if (blockIdx.x == 0) {
         if (threadIdx.x == 0) a.state->ov_count[a.ov_zero_slot] = 0;   // list of step k-1, refilled by step k+1
         overflow_pass(a, step);
     }
-    const float3 s = grid_shift(b, 0, step, a.state);
-    const float3 sn = grid_shift(b, 0, step + 1, a.state);
-    const bool sign = s.z > 0;
-    const uint32_t runs = (b.C + kRunCells - 1) / kRunCells;
+    // single box: geometry straight from the kernel parameters (constant bank)
+    const BoxDesc& b = SINGLE ? a.box0 : sbox;
+    float3 s = make_float3(0, 0, 0), sn = s;
+    if (SINGLE) {
+        s = grid_shift(b, 0, step, a.state);
+        sn = grid_shift(b, 0, step + 1, a.state);
+    }
+    int cur_box = -1;
     const uint32_t warps = gridDim.x * (uint32_t)kRunWarps;
     uint32_t run = blockIdx.x * (uint32_t)kRunWarps + (threadIdx.x >> 5);
-    uint32_t raw_next = 0;   // the count of this lane's cell, fetched one run ahead
-    if (run < runs && run * kRunCells + lane < b.C) raw_next = a.in_count[b.cell_base + run * kRunCells + lane];
-    if (lane < kBatchCells && raw_next)   // the first batch of the first run
-        prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(run * kRunCells + lane) * b.cap,
+    uint2 next = run_entry<SINGLE>(a, run);
+    uint32_t raw_next = lane < (next.y & 63u) ? a.in_count[next.x + lane] : 0u;   // counts one run ahead
+    if (SINGLE && lane < kBatchCells && raw_next)   // the first batch of the first run
+        prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(next.x - b.cell_base + lane) * b.cap,
                     min(raw_next, b.cap) * (uint32_t)sizeof(Slot));
 
-    for (; run < runs; run += warps) {
-        const uint32_t c = run * kRunCells + lane;
-        const bool valid = c < b.C;
-        const uint32_t cnt = min(raw_next, b.cap);
-        if (valid) a.zero_count[b.cell_base + c] = 0;   // counts of step k-1: step k+1 fills them
-        {
-            const uint32_t cn = c + warps * kRunCells;
-            raw_next = (run + warps < runs && cn < b.C) ? a.in_count[b.cell_base + cn] : 0u;
+    for (; run < a.num_runs; run += warps) {
+        const uint2 cur = next;
+        if (!SINGLE && (int)(cur.y >> 6) != cur_box) {   // box and grid shifts (drawn by the prologue)
+            cur_box = (int)(cur.y >> 6);
+            __syncwarp();
+            if (lane < sizeof(BoxDesc) / 16)
+                reinterpret_cast<uint4*>(&sbox)[lane] = __ldg(reinterpret_cast<const uint4*>(a.boxes + cur_box) + lane);
+            const float4 s0 = __ldg(a.box_shifts + 2 * cur_box), s1 = __ldg(a.box_shifts + 2 * cur_box + 1);
+            s = make_float3(s0.x, s0.y, s0.z);
+            sn = make_float3(s1.x, s1.y, s1.z);
+            __syncwarp();
         }
-        const Slot* const bucket0 = a.in_slots + b.slot_base + (uint64_t)run * kRunCells * b.cap;
+        const bool sign = s.z > 0;
+        const uint32_t c = cur.x - b.cell_base + lane;   // box-local cell of this lane
+        const bool valid = lane < (cur.y & 63u);
+        const uint32_t cnt = min(raw_next, b.cap);
+        if (valid) a.zero_count[cur.x + lane] = 0;   // counts of step k-1: step k+1 fills them
+        next = run_entry<SINGLE>(a, run + warps);
+        raw_next = lane < (next.y & 63u) ? a.in_count[next.x + lane] : 0u;
+        const Slot* const bucket0 = a.in_slots + b.slot_base + (uint64_t)(cur.x - b.cell_base) * b.cap;
         const uint3 cc = storage_coords(b, valid ? c : 0u);
         bool layer, wall;
         wall_layer(b, cc.z, sign, layer, wall);
@@ -1247,11 +1272,9 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a)
             if (c8 + kBatchCells < kRunCells) {
                 if (lane >= c8 + kBatchCells && lane < c8 + 2 * kBatchCells && cnt)
                     prefetch_l2(bucket0 + (uint64_t)lane * b.cap, cnt * (uint32_t)sizeof(Slot));
-            } else if (lane < kBatchCells && run + warps < runs && c + warps * kRunCells < b.C) {
-                const uint32_t nc = min(raw_next, b.cap);
-                if (nc)
-                    prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(c + warps * kRunCells) * b.cap,
-                                nc * (uint32_t)sizeof(Slot));
+            } else if (SINGLE && lane < kBatchCells && raw_next) {
+                prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(next.x - b.cell_base + lane) * b.cap,
+                            min(raw_next, b.cap) * (uint32_t)sizeof(Slot));
             }
             // exact sums of the batch's real particles: kBatchLanes lanes per cell
             {
@@ -1364,15 +1387,32 @@ __global__ void __launch_bounds__(kThreads) overflow_select_kernel(const StepArg
     // velocity, as step_kernel draws them, and stores the count and the exact
     // velocity sums.  Drawn here, every thread busy, instead of by a few lanes
     // of each run.
-    if (a.ghosts && a.box0.wall_z) {
-        const BoxDesc& b = a.box0;
-        const uint64_t step = a.step_base ? *a.step_base + a.step : a.step;
-        const float3 s = grid_shift(b, 0, step, a.state);
-        const float shift_abs = fabsf(s.z);
-        const bool sign = s.z > 0;
-        const uint32_t Lx = (uint32_t)b.L[0], Lz = (uint32_t)b.L[2];
-        const uint32_t walls = 2u * Lx * (uint32_t)b.L[1];
-        for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < walls; w += gridDim.x * blockDim.x) {
+    const uint64_t step = a.step_base ? *a.step_base + a.step : a.step;
+    if (a.run_kernel && a.box_shifts) {   // ensembles: every box's grid shifts of steps k and k+1
+        for (uint32_t bi = blockIdx.x * blockDim.x + threadIdx.x; bi < (uint32_t)a.nboxes; bi += gridDim.x * blockDim.x) {
+            const float3 s0 = grid_shift(a.boxes[bi], (int)bi, step, a.state);
+            const float3 s1 = grid_shift(a.boxes[bi], (int)bi, step + 1, a.state);
+            a.box_shifts[2 * bi] = make_float4(s0.x, s0.y, s0.z, 0.0f);
+            a.box_shifts[2 * bi + 1] = make_float4(s1.x, s1.y, s1.z, 0.0f);
+        }
+    }
+    if (a.run_kernel && a.ghosts) {
+        for (uint64_t wg = blockIdx.x * blockDim.x + threadIdx.x; wg < a.total_walls;
+             wg += (uint64_t)gridDim.x * blockDim.x) {
+            int bi = 0;   // the box of entry wg: the last with wall_base <= wg (boxes without walls add none)
+            if (a.nboxes > 1) {
+                int hi = a.nboxes - 1;
+                while (bi < hi) {
+                    const int mid = (bi + hi + 1) >> 1;
+                    if (a.boxes[mid].wall_base <= wg) bi = mid; else hi = mid - 1;
+                }
+            }
+            const BoxDesc& b = a.nboxes > 1 ? a.boxes[bi] : a.box0;
+            const float3 s = grid_shift(b, bi, step, a.state);
+            const float shift_abs = fabsf(s.z);
+            const bool sign = s.z > 0;
+            const uint32_t Lx = (uint32_t)b.L[0], Lz = (uint32_t)b.L[2];
+            const uint32_t w = (uint32_t)(wg - b.wall_base);
             const uint32_t col = w >> 1, y = fast_div(col, b.div_x), x = col - y * Lx;
             const uint32_t cz = (w & 1u) ? Lz - (sign ? 1u : 2u) : (sign ? 1u : 0u);
             bool layer, ghosts;
@@ -1393,7 +1433,7 @@ __global__ void __launch_bounds__(kThreads) overflow_select_kernel(const StepArg
                 r.sy = fixed24(v.y);
                 r.sz = fixed24(v.z);
             }
-            a.ghosts[b.wall_base + w] = r;
+            a.ghosts[wg] = r;
         }
     }
     const uint32_t n = min(a.state->ov_count[a.ov_in_slot], a.ov_cap);
@@ -1831,15 +1871,21 @@ const StepFn kStepFns[2][2][2][2] = {
 
 bool run_kernel_takes(const StepArgs& a, int algorithm, bool table)
 {
-    return algorithm == 0 && !table && a.nboxes == 1 && !a.replay && !a.tape_key && !a.pressure &&
-           a.box0.n <= kRunMaxN && (a.ghosts || !a.box0.wall_z);
+    return algorithm == 0 && !table && !a.replay && !a.tape_key && !a.pressure && (a.ghosts || !a.total_walls) &&
+           (a.nboxes == 1 || (a.run_info && a.box_shifts)) && a.boxes_n_max <= kRunMaxN;
 }
 
 cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st)
 {
-    if (run_kernel_takes(a, algorithm, table)) {
-        if (a.sample) srd_run_kernel<true><<<grid, kThreads, 0, st>>>(a);
-        else srd_run_kernel<false><<<grid, kThreads, 0, st>>>(a);
+    if (a.run_kernel) {
+        const bool single = a.nboxes == 1;
+        if (a.sample) {
+            if (single) srd_run_kernel<true, true><<<grid, kThreads, 0, st>>>(a);
+            else srd_run_kernel<true, false><<<grid, kThreads, 0, st>>>(a);
+        } else {
+            if (single) srd_run_kernel<false, true><<<grid, kThreads, 0, st>>>(a);
+            else srd_run_kernel<false, false><<<grid, kThreads, 0, st>>>(a);
+        }
         return cudaGetLastError();
     }
     const size_t smem = step_smem_bytes(pbuf, a.boxes_tile_cells, algorithm);
@@ -1882,7 +1928,8 @@ cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* bl
     e = cudaFuncGetAttributes(&attr, (const void*)advance_kernel);
     // the run kernel: about a quarter of the unified array as shared memory (4
     // CTAs of 14 KB), the rest L1, which holds each batch's slots between its two passes
-    for (const void* f : {(const void*)srd_run_kernel<false>, (const void*)srd_run_kernel<true>})
+    for (const void* f : {(const void*)srd_run_kernel<false, true>, (const void*)srd_run_kernel<true, true>,
+                          (const void*)srd_run_kernel<false, false>, (const void*)srd_run_kernel<true, false>})
         if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 27);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, (const void*)sample_finalize_kernel);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, (const void*)overflow_select_kernel);

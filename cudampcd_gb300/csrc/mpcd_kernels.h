@@ -16,9 +16,10 @@ size_t step_smem_bytes(uint32_t pbuf, uint32_t cells, int algorithm);
 cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* blocks_per_sm);
 // One step of every box (algorithm 0 = SRD, 1 = extended; table = injected draws).
 cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st);
-// Whether launch_step runs this step with srd_run_kernel (SRD, one box, Philox
-// draws, no replay, tape or pressure estimator, n <= 64, and the wall ghosts of
-// the step drawn by its prologue when the box has walls).
+// Whether srd_run_kernel can run this step (SRD, Philox draws, no replay, tape
+// or pressure estimator, n <= 64 in every box, a run table for ensembles and the
+// wall-ghost array when boxes have walls); the caller then sets a.run_kernel,
+// which launch_step and the step's prologue follow.
 bool run_kernel_takes(const StepArgs& a, int algorithm, bool table);
 // state->step_base += steps (the last node of a replayed step graph).
 cudaError_t launch_advance(DeviceState* state, unsigned steps, cudaStream_t st);

@@ -172,6 +172,14 @@ struct StepArgs {
     // srd_run_kernel steps: the wall ghosts of step k, drawn by the step's
     // prologue (overflow_select_kernel), entry wall_base + 2 (x + Lx y) + top
     GhostSum* ghosts;
+    // runs of up to 32 consecutive cells of one box (srd_run_kernel): per run
+    // {first global cell, cells | box << 6}; a single box computes them
+    const uint2* run_info;
+    uint32_t num_runs;
+    uint32_t boxes_n_max;         // the largest density of any box
+    uint64_t total_walls;         // wall-ghost entries of all boxes
+    float4* box_shifts;           // ensembles: grid shifts of steps k and k+1 per box (drawn by the prologue)
+    int32_t run_kernel;           // this step runs srd_run_kernel (the engine's choice, run_kernel_takes)
 };
 
 constexpr uint32_t kTapeNone = 0xFFFFFFFFu;
