@@ -353,6 +353,9 @@ def run_reference_cuda(args, rank, local_rank):
     p.algorithm = wl["algorithm"]
     p.collision_kernel = args.kernel
     p.device_id = local_rank
+    if args.physics in ("srd", "extended"):
+        run_reference_physics(args, p, pympcd, torch)
+        return
     t0 = time.perf_counter()
     sim = pympcd.Simulation(p, "cuda")
     torch.cuda.synchronize()
@@ -381,6 +384,60 @@ def run_reference_cuda(args, rank, local_rank):
                       "init_s": t_init,
                       "timing": "host wall clock around step(K) + synchronize (benchmark.py:53-66)"},
            "clocks": clocks.summary()}
+    print(json.dumps(out), flush=True)
+
+
+def run_reference_physics(args, p, pympcd, torch):
+    """The reference's own CUDA backend on the physics workload: warm-up, then 8
+    blocks of step_and_sample + get_mean_fields (the reference divides the sums by
+    S - 1, corrected here); viscosity from the curvature of each block's profile
+    and the density profile, the estimators run_physics applies to this backend.
+    The reference fills the fluid at n (Lz + 2) / Lz particles per cell
+    (backend_context.cu:19): with n = 16 and Lz = 32 that is 17, the density of this
+    backend's n = 17 run."""
+    import numpy as np
+
+    Lx, Ly, Lz = args.size or (256, 256, 32)
+    n, g, dt = args.n or 16, 0.0005, 0.02
+    p.n = n
+    p.volume_size = (Lx, Ly, Lz)
+    p.drag = g
+    p.algorithm = args.physics
+    sim = pympcd.Simulation(p, "cuda")
+    N = len(sim.get_particle_positions())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.step(args.warmup)
+    torch.cuda.synchronize()
+    t_warm = time.perf_counter() - t0
+    blocks, per = 8, max(2, args.steps // 8)
+    zc = np.arange(Lz + 2) + 0.5 - (Lz + 2) / 2.0
+    fluid = slice(1, Lz + 1)
+    A = np.stack([np.ones(Lz), -(zc[fluid] ** 2 + 1.0 / 12.0)], axis=1)
+    rho = N / (Lx * Ly * Lz)
+    etas, dens = [], np.zeros(Lz + 2)
+    for _ in range(blocks):
+        sim.step_and_sample(per)
+        d, v = sim.get_mean_fields()   # (x, y, z) and (x, y, z, 3)
+        u = np.asarray(v)[:, :, :, 0].mean(axis=(0, 1)) * (per - 1) / per
+        dens += np.asarray(d).mean(axis=(0, 1)) * (per - 1) / per / blocks
+        (a0, b0), *_ = np.linalg.lstsq(A, u[fluid], rcond=None)
+        etas.append(rho * g / (2.0 * b0))
+    etas = np.array(etas)
+    out = {"physics": args.physics, "impl": "reference-cuda", "kernel": args.kernel,
+           "workload": f"reference {args.physics} channel {Lx}x{Ly}x{Lz} cells + 2 walls, params.n={n} "
+                       f"(fluid density {rho:g}), T=1, dt={dt}, g={g}, N={N}",
+           "fluid_density": rho, "warmup_steps": args.warmup, "sampled_steps": blocks * per, "warmup_s": t_warm,
+           "ms_per_step_warmup": 1e3 * t_warm / max(1, args.warmup),
+           "viscosity": {"mean": float(etas.mean()), "stderr": float(etas.std(ddof=1) / np.sqrt(blocks)),
+                         "blocks": [float(e) for e in etas]},
+           "density_profile_fluid": {"mean": float(dens[fluid].mean()), "min": float(dens[fluid].min()),
+                                     "max": float(dens[fluid].max()), "first_layers": [float(x) for x in dens[1:5]],
+                                     "layers": [float(x) for x in dens]},
+           "velocity_profile": [float(x) for x in u],
+           "wall_pressure": None,
+           "wall_pressure_note": "the reference has no pressure measurement and its state between steps does not "
+                                 "carry the bounce-back and collision momentum the estimator sums"}
     print(json.dumps(out), flush=True)
 
 
@@ -598,7 +655,7 @@ def run_physics(args):
 
     alg = 1 if args.physics == "extended" else 0
     Lx, Ly, Lz = (args.size or (256, 256, 64))
-    n, g, dt = 20, 0.0005, 0.02
+    n, g, dt = args.n or 20, 0.0005, 0.02
     h = capi.Handle(L=(Lx, Ly, Lz + 2), periodic=(1, 1, 0), n=n, dt=dt, drag=g, algorithm=alg, seed=0)
     if args.eta_guess:   # start from the steady profile of a guessed viscosity: a shorter warm-up
         vel = h.velocities()
@@ -629,8 +686,9 @@ def run_physics(args):
         etas.append(n * g / (2.0 * b))
     etas, P = np.array(etas), np.array(P)
     srd_theory = (1 - np.cos(2 * np.pi / 3)) / (18 * dt) * (n - 1 + np.exp(-n))
-    out = {"physics": args.physics, "workload": f"{args.physics} channel {Lx}x{Ly}x{Lz} cells + 2 walls, n={n}, "
-                                                f"T=1, dt={dt}, g={g}, N={h.N}",
+    out = {"physics": args.physics, "impl": "gb300",
+           "workload": f"{args.physics} channel {Lx}x{Ly}x{Lz} cells + 2 walls, n={n}, T=1, dt={dt}, g={g}, N={h.N}",
+           "fluid_density": n, "ms_per_step_warmup": 1e3 * t_warm / max(1, args.warmup),
            "warmup_steps": args.warmup, "sampled_steps": blocks * per, "warmup_s": t_warm,
            "initial_profile_eta": args.eta_guess,
            "wall_pressure": {"mean": float(P.mean()), "stderr": float(P.std(ddof=1) / np.sqrt(blocks)),
@@ -638,7 +696,9 @@ def run_physics(args):
            "viscosity": {"mean": float(etas.mean()), "stderr": float(etas.std(ddof=1) / np.sqrt(blocks)),
                          "srd_theory": float(srd_theory), "blocks": [float(e) for e in etas]},
            "density_profile_fluid": {"mean": float(dens[fluid].mean()), "min": float(dens[fluid].min()),
-                                     "max": float(dens[fluid].max()), "first_layers": [float(x) for x in dens[1:5]]},
+                                     "max": float(dens[fluid].max()), "first_layers": [float(x) for x in dens[1:5]],
+                                     "layers": [float(x) for x in dens]},
+           "velocity_profile": [float(x) for x in u],
            "device_counters": {"bucket_overflows": h.counters()[0], "error_flags": h.counters()[1]}}
     h.close()
     print(json.dumps(out), flush=True)
@@ -760,6 +820,7 @@ def main():
     ap.add_argument("--small-replicas", dest="small_replicas", action="store_true")
     ap.add_argument("--physics", choices=["extended", "srd", "viscosity"])
     ap.add_argument("--eta-guess", dest="eta_guess", type=float, default=0.0)
+    ap.add_argument("--n", type=int, default=0, help="particles per cell of the physics workloads")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")
@@ -772,6 +833,8 @@ def main():
         run_ensemble(args)
     elif args.physics == "viscosity":
         run_viscosity(args)
+    elif args.physics and args.impl == "reference-cuda":
+        run_reference_cuda(args, rank, local_rank)
     elif args.physics:
         run_physics(args)
     elif args.impl == "reference":
