@@ -648,6 +648,79 @@ def run_ensemble(args):
     print(json.dumps(out), flush=True)
 
 
+def run_ensemble_viscosity(args):
+    """Per-replica SRD viscosity of the batched workload's replicas, as one batched
+    handle.  The replicas are those of ensemble_boxes(R) whose fluid height is at most
+    --max-height (the slowest mode of a taller channel relaxes over more steps than a
+    bounded run takes).  Each starts from the Poiseuille profile of 0.9 x the analytic
+    viscosity, so that a measurement pulled towards its start would read low; after
+    the warm-up, 4 sampled blocks give each replica's viscosity from the curvature of
+    its profile, with the spread of the blocks as its error.  A replica counts as
+    relaxed when the warm-up is at least 3 of its slowest relaxation times
+    L^2 n / (pi^2 eta dt) steps (the start's 10 % error is then below 0.5 %)."""
+    import math
+
+    import numpy as np
+
+    from cudampcd_gb300 import capi
+
+    boxes = [b for b in ensemble_boxes(args.ensemble) if b["L"][2] - 2 <= args.max_height]
+    h = capi.Handle(boxes=boxes)
+    alpha = 2 * math.pi / 3
+    theory = [(1 - math.cos(alpha)) / (18 * b["dt"]) * (b["n"] - 1 + math.exp(-b["n"])) for b in boxes]
+    pos, vel = h.positions(), h.velocities()
+    ranges = [h.box_range(r) for r in range(len(boxes))]
+    for b, eta, (p0, nr, _, _) in zip(boxes, theory, ranges):
+        hz = (b["L"][2] - 2) / 2.0
+        z = pos[p0:p0 + nr, 2].astype(np.float64)
+        vel[p0:p0 + nr, 0] += (b["n"] * b["drag"] * (hz * hz - z * z) / (2.0 * 0.9 * eta)).astype(np.float32)
+    h.set_velocities(vel)
+    del pos, vel
+    t0 = time.perf_counter()
+    h.step(args.warmup)
+    blocks, per = 4, max(2, args.steps // 4)
+    etas = np.zeros((blocks, len(boxes)))
+    for k in range(blocks):
+        h.step_and_sample(per)
+        _, v = h.sample_mean()
+        for r, (b, (_, _, c0, cr)) in enumerate(zip(boxes, ranges)):
+            Lx, Ly, Lz = b["L"]
+            u = v[c0:c0 + cr, 0].reshape(Lz, Ly, Lx).mean(axis=(1, 2)).astype(np.float64) * (per - 1) / per
+            zc = np.arange(Lz) + 0.5 - Lz / 2.0
+            A = np.stack([np.ones(Lz - 2), -(zc[1:-1] ** 2 + 1.0 / 12.0)], axis=1)
+            (_, curv), *_ = np.linalg.lstsq(A, u[1:-1], rcond=None)
+            etas[k, r] = b["n"] * b["drag"] / (2.0 * curv)
+    elapsed = time.perf_counter() - t0
+    flags = h.counters()[1]
+    h.close()
+    eta, err = etas.mean(axis=0), etas.std(axis=0, ddof=1) / np.sqrt(blocks)
+    rows, pulls, relaxed_dev = [], [], []
+    for r, b in enumerate(boxes):
+        Lf = b["L"][2] - 2
+        tau = Lf * Lf * b["n"] / (math.pi ** 2 * theory[r] * b["dt"])
+        relaxed = args.warmup >= 3 * tau
+        dev = eta[r] / theory[r] - 1
+        rows.append({"L": list(b["L"]), "n": b["n"], "drag": b["drag"], "eta": float(eta[r]), "stderr": float(err[r]),
+                     "theory": theory[r], "deviation": float(dev), "tau_steps": tau, "relaxed": bool(relaxed)})
+        if relaxed:
+            pulls.append((eta[r] - theory[r]) / err[r])
+            relaxed_dev.append(dev)
+    pulls, relaxed_dev = np.array(pulls), np.array(relaxed_dev)
+    precise = [row for row in rows if row["relaxed"] and row["stderr"] < 0.01 * row["theory"]]
+    out = {"physics": "ensemble viscosity",
+           "workload": f"{len(boxes)} of the {args.ensemble} batched-workload replicas (fluid height <= "
+                       f"{args.max_height}), one batched handle, start at 0.9 x the analytic profile",
+           "warmup_steps": args.warmup, "sampled_steps": blocks * per, "seconds": elapsed, "error_flags": flags,
+           "relaxed_replicas": int(len(pulls)),
+           "relaxed": {"mean_deviation": float(relaxed_dev.mean()) if len(pulls) else None,
+                       "pull_mean": float(pulls.mean()) if len(pulls) else None,
+                       "pull_std": float(pulls.std(ddof=1)) if len(pulls) > 1 else None},
+           "precise_replicas": len(precise),
+           "precise_within_2pct": sum(abs(row["deviation"]) < 0.02 for row in precise),
+           "replicas": rows}
+    print(json.dumps(out), flush=True)
+
+
 def run_physics(args):
     import numpy as np
 
@@ -821,6 +894,8 @@ def main():
     ap.add_argument("--physics", choices=["extended", "srd", "viscosity"])
     ap.add_argument("--eta-guess", dest="eta_guess", type=float, default=0.0)
     ap.add_argument("--n", type=int, default=0, help="particles per cell of the physics workloads")
+    ap.add_argument("--viscosity", action="store_true", help="with --ensemble: per-replica viscosity")
+    ap.add_argument("--max-height", dest="max_height", type=int, default=74)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")
@@ -829,6 +904,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
     if args.adjoint:
         run_adjoint(args)
+    elif args.ensemble and args.viscosity:
+        run_ensemble_viscosity(args)
     elif args.ensemble:
         run_ensemble(args)
     elif args.physics == "viscosity":

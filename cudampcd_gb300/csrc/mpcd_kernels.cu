@@ -1604,7 +1604,10 @@ __global__ void __launch_bounds__(kThreads) scan_kernel(const uint32_t* count, c
                 if (flag == kFlagPre) break;
                 --t;
             }
-            if (timed_out) atomicOr(&state->error_flags, kErrWaitTimeout);
+            if (timed_out) {
+                atomicOr(&state->error_flags, kErrWaitTimeout);
+                __threadfence();   // the flag is visible before the (incomplete) prefix is
+            }
             atomicExch(status + tile, kFlagPre | (uint32_t)(prefix + total));
         }
         s_prefix = prefix;
@@ -1618,8 +1621,13 @@ __global__ void __launch_bounds__(kThreads) scan_kernel(const uint32_t* count, c
         run += v[k];
     }
     if (tile == (uint32_t)((cells + kThreads * kScanItems - 1) / (kThreads * kScanItems)) - 1 &&
-        threadIdx.x == kThreads - 1)
-        offsets[cells] = s_prefix + total;
+        threadIdx.x == kThreads - 1) {
+        // a look-back that gave up anywhere before this tile published an incomplete
+        // prefix: mark the result invalid in the buffer itself
+        __threadfence();
+        const bool bad = (atomicAdd(&state->error_flags, 0u) & kErrWaitTimeout) != 0;
+        offsets[cells] = bad ? 0xFFFFFFFFu : s_prefix + total;
+    }
 }
 
 // Layout dump: the particles of every cell, in stable order, cells in storage

@@ -275,7 +275,12 @@ int32_t mpcd_gb_profile_tape(mpcd_gb_handle *h, uint32_t *key, uint32_t *lab, ui
  * both results are undefined: calls queued on one stream are ordered and safe, calls on
  * different streams, handles or host threads of one device must be serialised by the
  * caller.  A look-back wait that times out sets error bit 1 (mpcd_gb_counters), which
- * the next mpcd_gb_step, mpcd_gb_step_and_sample or setter reports as MPCD_GB_EDEVICE. */
+ * the next mpcd_gb_step, mpcd_gb_step_and_sample or setter reports as MPCD_GB_EDEVICE,
+ * and makes the call write 0xFFFFFFFF to d_offsets[C] in place of the particle count:
+ * a caller that reads the offsets every step can tell a bad result from the buffer
+ * alone.  The scratch address found at set-up is kept for the life of the process:
+ * after cudaDeviceReset on that device (which frees the library's device memory) the
+ * entry point must not be called again. */
 int32_t mpcd_gb_cell_offsets_noalloc(mpcd_gb_handle *h, uint32_t *d_offsets, uint64_t n_offsets);
 
 #ifdef __cplusplus
