@@ -812,6 +812,12 @@ private:
             b.slot_base = slots;
             b.dense_base = particles;
             b.wall_base = walls;
+            // run-kernel batches of about 80-96 particles: 16 cells up to n = 6, 8 up to 12, else 4
+            b.run_batch = b.n <= 6 ? 16u : (b.n <= 12 ? 8u : 4u);
+            if (const char* e = std::getenv("MPCD_GB_RUN_BATCH")) {   // tuning sweeps
+                const uint32_t v = (uint32_t)std::strtoul(e, nullptr, 10);
+                if (v == 4 || v == 8 || v == 16) b.run_batch = v;
+            }
             if (b.wall_z) walls += 2ull * (uint64_t)b.L[0] * (uint64_t)b.L[1];
             cells += b.C;
             slots += (uint64_t)b.C * b.cap;
@@ -898,13 +904,20 @@ private:
                 tile_info_.push_back({b.cell_base + t * tc, std::min(tc, b.C - t * tc) | (tc << 16), (uint32_t)r, 0u});
         }
         tiles_ = tiles;
-        // runs of up to 32 cells of one box (srd_run_kernel): {first cell, cells | box << 6}
+        // runs of up to 32 cells of one box (srd_run_kernel): {first cell, cells | box << 6},
+        // listed by batch class (16, 8, then 4 cells per batch; one launch per class)
         run_info_.clear();
-        for (size_t r = 0; r < boxes_.size(); ++r) {
-            const BoxDesc& b = boxes_[r];
-            for (uint32_t c = 0; c < b.C; c += 32)
-                run_info_.push_back(make_uint2(b.cell_base + c, std::min(32u, b.C - c) | ((uint32_t)r << 6)));
+        for (int cls = 0; cls < 3; ++cls) {
+            run_class_[cls] = (uint32_t)run_info_.size();
+            const uint32_t batch = 16u >> cls;
+            for (size_t r = 0; r < boxes_.size(); ++r) {
+                const BoxDesc& b = boxes_[r];
+                if (b.run_batch != batch) continue;
+                for (uint32_t c = 0; c < b.C; c += 32)
+                    run_info_.push_back(make_uint2(b.cell_base + c, std::min(32u, b.C - c) | ((uint32_t)r << 6)));
+            }
         }
+        run_class_[3] = (uint32_t)run_info_.size();
         pbuf_ = pbuf;
         fill_ = fill;
         for (auto& g : graph_) g.reset();   // graphs bake the tiling into their launches
@@ -1015,6 +1028,7 @@ private:
         a.tile_info = tile_info_d_.as<TileEntry>();
         a.run_info = boxes_.size() > 1 ? run_info_d_.as<uint2>() : nullptr;
         a.num_runs = (uint32_t)run_info_.size();
+        for (int c = 0; c < 4; ++c) a.run_class[c] = run_class_[c];
         a.boxes_n_max = n_max_;
         a.total_walls = walls_;
         a.ghosts = ghosts_.as<GhostSum>();
@@ -1315,6 +1329,7 @@ private:
     std::vector<TileEntry> tile_info_;   // tile table of the current tiling
     DeviceBuffer tile_info_d_;
     std::vector<uint2> run_info_;        // run table of srd_run_kernel
+    uint32_t run_class_[4] = {0, 0, 0, 0};
     DeviceBuffer run_info_d_;
     uint32_t n_max_ = 0;
     DeviceBuffer ov_head_[2], ov_next_[2];   // overflow chains: heads by cell, links by entry (by step parity)

@@ -1143,8 +1143,9 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
 // buckets (a cell's bucket is contiguous).  Per run:
 //   per cell (its lane): count, wall ghosts (drawn by the step's prologue),
 //   rotation axis;
-//   then batches of 8 cells: exact velocity sums of the batch's particles (4
-//   lanes per cell, four loads in flight each), and per particle, 32
+//   then batches of 4, 8 or 16 cells (about 80 particles): exact velocity sums of
+//   the batch's particles (32 / batch lanes per cell, four loads in flight each),
+//   and per particle, 32
 //   consecutive particles of the batch at a time (their slots still in L1 from
 //   the sums): the collision, unshift, drag, lab-grid sample, streaming of step
 //   k+1 and its cell, the slot claim (warp-aggregated) and one 256-bit store.
@@ -1153,10 +1154,9 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
 // by step_kernel (the getters) reproduces it bit for bit.
 
 constexpr uint32_t kRunCells = 32;
-constexpr uint32_t kBatchCells = 4;                   // cells summed and finished together
-constexpr uint32_t kBatchLanes = 32 / kBatchCells;    // lanes per cell in the sums
-static_assert(kBatchCells >= 2 && kBatchCells <= 16 && (kBatchCells & (kBatchCells - 1)) == 0,
-              "batches of a power of two of cells, searched by halving");
+// Cells summed and finished together: BATCH = 4, 8 or 16, about 80 particles per
+// batch (the engine picks it from n: a box's run_batch); 32 / BATCH lanes per cell in
+// the sums.
 constexpr int kRunWarps = kThreads / 32;
 constexpr uint32_t kRunMaxN = 64;                     // densities this kernel takes
 
@@ -1190,8 +1190,9 @@ __device__ __forceinline__ uint2 run_entry(const StepArgs& a, uint32_t run)
     return make_uint2(a.box0.cell_base + c0, min(kRunCells, a.box0.C - c0));
 }
 
-template <bool SAMPLE, bool SINGLE>
-__global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a)
+template <bool SAMPLE, bool SINGLE, uint32_t BATCH>
+__global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, uint32_t run_begin, uint32_t run_end,
+                                                              bool first_launch)
 {
     __shared__ RunShared shared_runs[kRunWarps];
     __shared__ __align__(16) BoxDesc shared_box[SINGLE ? 1 : kRunWarps];   // ensembles: the box of the warp's run
@@ -1200,10 +1201,13 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a)
     BoxDesc& sbox = shared_box[SINGLE ? 0 : threadIdx.x >> 5];
     const uint64_t step = a.step_base ? *a.step_base + a.step : a.step;   // graph replays read the base
 
-    if (blockIdx.x == 0) {
+    if (blockIdx.x == 0 && first_launch) {   // once per step (ensembles launch once per batch size)
         if (threadIdx.x == 0) a.state->ov_count[a.ov_zero_slot] = 0;   // list of step k-1, refilled by step k+1
         overflow_pass(a, step);
     }
+    constexpr uint32_t kBatchCells = BATCH;
+    constexpr uint32_t kBatchLanes = 32 / BATCH;   // lanes per cell in the sums
+    static_assert(BATCH == 4 || BATCH == 8 || BATCH == 16, "batches of 4, 8 or 16 cells");
     // single box: geometry straight from the kernel parameters (constant bank)
     const BoxDesc& b = SINGLE ? a.box0 : sbox;
     float3 s = make_float3(0, 0, 0), sn = s;
@@ -1213,14 +1217,14 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a)
     }
     int cur_box = -1;
     const uint32_t warps = gridDim.x * (uint32_t)kRunWarps;
-    uint32_t run = blockIdx.x * (uint32_t)kRunWarps + (threadIdx.x >> 5);
-    uint2 next = run_entry<SINGLE>(a, run);
+    uint32_t run = run_begin + blockIdx.x * (uint32_t)kRunWarps + (threadIdx.x >> 5);
+    uint2 next = run_entry<SINGLE>(a, run < run_end ? run : a.num_runs);
     uint32_t raw_next = lane < (next.y & 63u) ? a.in_count[next.x + lane] : 0u;   // counts one run ahead
     if (SINGLE && lane < kBatchCells && raw_next)   // the first batch of the first run
         prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(next.x - b.cell_base + lane) * b.cap,
                     min(raw_next, b.cap) * (uint32_t)sizeof(Slot));
 
-    for (; run < a.num_runs; run += warps) {
+    for (; run < run_end; run += warps) {
         const uint2 cur = next;
         if (!SINGLE && (int)(cur.y >> 6) != cur_box) {   // box and grid shifts (drawn by the prologue)
             cur_box = (int)(cur.y >> 6);
@@ -1237,7 +1241,7 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a)
         const bool valid = lane < (cur.y & 63u);
         const uint32_t cnt = min(raw_next, b.cap);
         if (valid) a.zero_count[cur.x + lane] = 0;   // counts of step k-1: step k+1 fills them
-        next = run_entry<SINGLE>(a, run + warps);
+        next = run_entry<SINGLE>(a, run + warps < run_end ? run + warps : a.num_runs);
         raw_next = lane < (next.y & 63u) ? a.in_count[next.x + lane] : 0u;
         const Slot* const bucket0 = a.in_slots + b.slot_base + (uint64_t)(cur.x - b.cell_base) * b.cap;
         const uint3 cc = storage_coords(b, valid ? c : 0u);
@@ -1877,6 +1881,14 @@ const StepFn kStepFns[2][2][2][2] = {
       {step_kernel<1, true, true, false>, step_kernel<1, true, true, true>}}}};
 }  // namespace
 
+using StepFnRun = void (*)(const StepArgs, uint32_t, uint32_t, bool);
+// [sample][single box][batch class: 16, 8, 4 cells]
+static const StepFnRun kRunFns[2][2][3] = {
+    {{srd_run_kernel<false, false, 16>, srd_run_kernel<false, false, 8>, srd_run_kernel<false, false, 4>},
+     {srd_run_kernel<false, true, 16>, srd_run_kernel<false, true, 8>, srd_run_kernel<false, true, 4>}},
+    {{srd_run_kernel<true, false, 16>, srd_run_kernel<true, false, 8>, srd_run_kernel<true, false, 4>},
+     {srd_run_kernel<true, true, 16>, srd_run_kernel<true, true, 8>, srd_run_kernel<true, true, 4>}}};
+
 bool run_kernel_takes(const StepArgs& a, int algorithm, bool table)
 {
     return algorithm == 0 && !table && !a.replay && !a.tape_key && !a.pressure && (a.ghosts || !a.total_walls) &&
@@ -1886,15 +1898,19 @@ bool run_kernel_takes(const StepArgs& a, int algorithm, bool table)
 cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st)
 {
     if (a.run_kernel) {
-        const bool single = a.nboxes == 1;
-        if (a.sample) {
-            if (single) srd_run_kernel<true, true><<<grid, kThreads, 0, st>>>(a);
-            else srd_run_kernel<true, false><<<grid, kThreads, 0, st>>>(a);
-        } else {
-            if (single) srd_run_kernel<false, true><<<grid, kThreads, 0, st>>>(a);
-            else srd_run_kernel<false, false><<<grid, kThreads, 0, st>>>(a);
+        // one launch per batch size in use: a single box's, or an ensemble's density
+        // classes, whose runs the run table lists class by class
+        bool first = true;
+        for (int cls = 0; cls < 3; ++cls) {
+            const uint32_t r0 = a.run_class[cls], r1 = a.run_class[cls + 1];
+            if (r0 >= r1) continue;
+            const StepFnRun f = kRunFns[a.sample ? 1 : 0][a.nboxes == 1 ? 1 : 0][cls];
+            f<<<grid, kThreads, 0, st>>>(a, r0, r1, first);
+            first = false;
+            const cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
         }
-        return cudaGetLastError();
+        return cudaSuccess;
     }
     const size_t smem = step_smem_bytes(pbuf, a.boxes_tile_cells, algorithm);
     kStepFns[algorithm ? 1 : 0][table ? 1 : 0][a.nboxes == 1 ? 1 : 0][a.replay ? 1 : 0]<<<grid, kThreads, smem, st>>>(
@@ -1936,9 +1952,12 @@ cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* bl
     e = cudaFuncGetAttributes(&attr, (const void*)advance_kernel);
     // the run kernel: about a quarter of the unified array as shared memory (4
     // CTAs of 14 KB), the rest L1, which holds each batch's slots between its two passes
-    for (const void* f : {(const void*)srd_run_kernel<false, true>, (const void*)srd_run_kernel<true, true>,
-                          (const void*)srd_run_kernel<false, false>, (const void*)srd_run_kernel<true, false>})
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 27);
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j)
+            for (int k = 0; k < 3; ++k)
+                if (e == cudaSuccess)
+                    e = cudaFuncSetAttribute((const void*)kRunFns[i][j][k], cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             27);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, (const void*)sample_finalize_kernel);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, (const void*)overflow_select_kernel);
     if (e != cudaSuccess) return e;

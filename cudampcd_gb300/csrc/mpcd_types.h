@@ -55,7 +55,8 @@ struct BoxDesc {
     uint64_t div_z, div_x; // ceil(2^48 / Lz), ceil(2^48 / Lx): exact division of cell indices < 2^31
     uint32_t seed_lo, seed_hi;
     uint64_t wall_base;    // first wall-ghost entry of this box (2 per column, with walls in z)
-    uint64_t unused;
+    uint32_t run_batch;    // srd_run_kernel: cells summed and finished together (4, 8 or 16)
+    uint32_t unused;
 };
 
 // The step kernel copies a box descriptor into shared memory 16 bytes per thread.
@@ -176,6 +177,7 @@ struct StepArgs {
     // {first global cell, cells | box << 6}; a single box computes them
     const uint2* run_info;
     uint32_t num_runs;
+    uint32_t run_class[4];        // runs [run_class[c], run_class[c+1]) take batches of 16, 8, 4 cells (c = 0, 1, 2)
     uint32_t boxes_n_max;         // the largest density of any box
     uint64_t total_walls;         // wall-ghost entries of all boxes
     float4* box_shifts;           // ensembles: grid shifts of steps k and k+1 per box (drawn by the prologue)
