@@ -58,6 +58,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -502,6 +503,18 @@ def run_e2e(args, wl, algorithm, rank, local_rank, dist, world, N):
             "api": "cudampcd_gb300.Simulation.step_and_sample + get_mean_fields (host wall clock)"}
 
 
+def device_memory(handle_bytes: int, n: int, cells: int, particles: int) -> dict:
+    """Device memory of one handle: measured (free memory before creation minus
+    after the warm-up steps) and the two bucket sets' share: cells x depth slots of
+    32 B, depth = min(4n, n + ceil(4 sqrt(n)) + 2), plus the extension area
+    (min(N, 2^22) slots, at least 4n)."""
+    depth = min(4 * n, n + math.ceil(4 * math.sqrt(n)) + 2)
+    ext = max(4 * n, min(particles, 1 << 22))
+    return {"handle_gb": handle_bytes / 1e9, "bucket_depth": depth, "bucket_depth_reference": 4 * n,
+            "buckets_gb": 2 * 32 * (cells * depth + ext) / 1e9,
+            "buckets_gb_at_reference_depth": 2 * 32 * cells * 4 * n / 1e9}
+
+
 def run_gpu_arm(args, rank, world, local_rank):
     import torch
 
@@ -527,12 +540,14 @@ def run_gpu_arm(args, rank, world, local_rank):
             wl["L"] = (args.size[0], args.size[1], args.size[2] + 2)
         workload_name = (f"{args.algorithm.upper()} Poiseuille channel {wl['L'][0]}x{wl['L'][1]}x{wl['L'][2] - 2} "
                          f"cells (+2 wall layers in z), n={wl['n']}, T=1, g=0.001, dt=0.02, Philox seed 0")
+    free_before = torch.cuda.mem_get_info(local_rank)[0]
     h = capi.Handle(L=wl["L"], periodic=wl["periodic"], n=wl["n"], dt=wl["dt"], drag=wl["drag"],
                     temperature=wl["temperature"], algorithm=algorithm, seed=wl["seed"] + rank,
                     device_id=local_rank)
     N, C = h.N, h.C
     h.step(args.warmup)
     h.synchronize()
+    memory = device_memory(free_before - torch.cuda.mem_get_info(local_rank)[0], wl["n"], C, N)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -573,6 +588,7 @@ def run_gpu_arm(args, rank, world, local_rank):
             "clocks": clocks.summary(),
             "gpu_launches": 2 * args.steps,   # per step: overflow selection, step kernel
             "device_counters": {"bucket_overflows": overflowed, "error_flags": flags},
+            "device_memory": memory,
         }
         if ref_gpu is not None:
             if "value" in ref_gpu:

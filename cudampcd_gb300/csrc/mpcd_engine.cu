@@ -550,13 +550,11 @@ public:
               "cell offsets");
     }
 
-    // The overflow list is filled in arrival order; order its part of a dump by
-    // (cell, id) so that a dump is deterministic.
+    // The overflow list is filled in arrival order; order its part of a dump (the
+    // last layout_tail_ entries) by (cell, id) so that a dump is deterministic.
     void sort_overflow_tail(uint32_t* cell, uint32_t* slot, uint32_t* id)
     {
-        DeviceState st;
-        check(cudaMemcpy(&st, state_.p, sizeof st, cudaMemcpyDeviceToHost), "dump");
-        const uint64_t m = std::min(st.ov_count[step_ % 3], ov_cap_);
+        const uint64_t m = layout_tail_;
         if (m < 2) return;
         const uint64_t base = N_ - m;
         std::vector<uint64_t> order(m);
@@ -788,6 +786,13 @@ private:
         b.cos_a = cosf((float)((M_PI * 120) / 180));
         b.n = p.n;
         b.cap = 4 * p.n;
+        // bucket depth: n + 4 sqrt(n) + 2 (a Poisson(n) cell exceeds it in about 1 of
+        // 10^4..10^5 cells), at most the reference's 4n
+        b.depth = std::min(b.cap, p.n + (uint32_t)std::ceil(4.0 * std::sqrt((double)p.n)) + 2u);
+        if (const char* e = std::getenv("MPCD_GB_BUCKET_DEPTH")) {   // test hook: force spills
+            const uint32_t v = (uint32_t)std::strtoul(e, nullptr, 10);
+            if (v >= 1) b.depth = std::min(b.cap, v);
+        }
         const uint64_t C = (uint64_t)b.L[0] * b.L[1] * b.L[2];
         if (C >= (1ull << 31)) throw Error(MPCD_GB_EINVAL, "too many cells");
         if (Nf >= (1ull << 32) - 1) throw Error(MPCD_GB_EINVAL, "too many particles");
@@ -820,7 +825,7 @@ private:
             }
             if (b.wall_z) walls += 2ull * (uint64_t)b.L[0] * (uint64_t)b.L[1];
             cells += b.C;
-            slots += (uint64_t)b.C * b.cap;
+            slots += (uint64_t)b.C * b.depth;
             particles += b.N;
             n_max = std::max(n_max, b.n);
             boxes_.push_back(b);
@@ -832,8 +837,13 @@ private:
         n_max_ = n_max;
         total_slots_ = slots;
         ov_cap_ = (uint32_t)std::max<uint64_t>(1u << 16, std::min<uint64_t>(N_, 1u << 22));
-        if (total_slots_ + ov_cap_ >= (1ull << 32))
-            throw Error(MPCD_GB_EINVAL, "cells * 4n exceeds the 32-bit slot space of one handle");
+        // extension area: the colliding sets of the cells past their depth (at most N
+        // particles in all; at least one cell's 4n)
+        uint32_t cap_max = 0;
+        for (const BoxDesc& b : boxes_) cap_max = std::max(cap_max, b.cap);
+        ext_cap_ = (uint32_t)std::max<uint64_t>(cap_max, std::min<uint64_t>(N_, 1u << 22));
+        if (total_slots_ + ext_cap_ + ov_cap_ >= (1ull << 32))
+            throw Error(MPCD_GB_EINVAL, "bucket slots exceed the 32-bit slot space of one handle");
         // tiles: per box a power-of-two number of cells (a group of 256 / cells
         // threads per cell) holding up to pbuf particles on average; the buffer
         // holds one cell with all its ghosts (cap + n = 5n) at least.  The
@@ -949,7 +959,7 @@ private:
         check(boxes_d_.alloc(sizeof(BoxDesc) * boxes_.size()), "alloc boxes");
         upload_tiling();
         for (int k = 0; k < 2; ++k) {
-            check(slots_[k].alloc(sizeof(Slot) * total_slots_), "alloc buckets");
+            check(slots_[k].alloc(sizeof(Slot) * (total_slots_ + ext_cap_)), "alloc buckets");
             check(ov_pos_[k].alloc(sizeof(float4) * ov_cap_), "alloc overflow list");
             check(ov_vel_[k].alloc(sizeof(float4) * ov_cap_), "alloc overflow list");
             check(ov_next_[k].alloc(sizeof(uint32_t) * ov_cap_), "alloc overflow chains");
@@ -1034,6 +1044,7 @@ private:
         a.ghosts = ghosts_.as<GhostSum>();
         a.box_shifts = boxes_.size() > 1 ? box_shifts_.as<float4>() : nullptr;
         a.total_slots = total_slots_;
+        a.ext_cap = ext_cap_;
         a.step = k;
         const unsigned p = (unsigned)(k & 1), q = p ^ 1u;
         a.in_slots = slots_[p].as<Slot>();
@@ -1140,6 +1151,7 @@ private:
     {
         const unsigned p = (unsigned)(k & 1);
         return launch_overflow_select(a, slots_[p].as<Slot>(), ov_pos_[p].as<float4>(), ov_vel_[p].as<float4>(),
+                                      ov_head_[p].as<uint32_t>(),
                                       a.run_kernel && (a.total_walls || a.box_shifts) ? sms_ * 8 : sms_, st);
     }
 
@@ -1238,6 +1250,9 @@ private:
                                   0, sizeof(unsigned int), stream_),
                   "clear overflow list");
         }
+        check(cudaMemsetAsync((char*)state_.p + offsetof(DeviceState, ext_count) + sizeof(unsigned int) * (k & 1), 0,
+                              sizeof(unsigned int), stream_),
+              "clear extension");
         StepArgs a = args(k - 1);   // out_* = buckets, counts and overflow list of step k
         a.tape_lab = tape_b0;
         check(launch_scatter(a, dense_pos_.as<float>(), dense_vel_.as<float>(), N_, sms_ * 8, stream_),
@@ -1249,18 +1264,21 @@ private:
     {
         const unsigned p = parity();
         StepArgs a = args(step_);
+        check(select_overflow(a, step_, stream_), "overflow selection");   // the step's own selection repeats nothing
         check(launch_layout(a, count_[step_ % 3].as<uint32_t>(), slots_[p].as<Slot>(),
                             offsets_.as<uint32_t>(), cells_, N_, scan_status_.as<unsigned long long>(),
                             scan_counter_.as<unsigned int>(), ov_pos_[p].as<float4>(), ov_vel_[p].as<float4>(),
                             (unsigned)(step_ % 3), cell, slot, prev, id, sms_ * 8, stream_),
               "layout");
-        uint32_t total = 0;
+        uint32_t total = 0, tail = 0;
         check(cudaMemcpyAsync(&total, offsets_.as<uint32_t>() + cells_, sizeof total, cudaMemcpyDeviceToHost, stream_),
               "layout");
-        DeviceState st;
-        check(cudaMemcpyAsync(&st, state_.p, sizeof st, cudaMemcpyDeviceToHost, stream_), "layout");
+        check(cudaMemcpyAsync(&tail, scan_counter_.as<unsigned int>(), sizeof tail, cudaMemcpyDeviceToHost, stream_),
+              "layout");
         check(cudaStreamSynchronize(stream_), "layout");
-        expect_count((uint64_t)total + std::min(st.ov_count[step_ % 3], ov_cap_));
+        check_device_errors();
+        layout_tail_ = tail;
+        expect_count((uint64_t)total + tail);
     }
 
     void expect_count(uint64_t have)
@@ -1298,6 +1316,7 @@ private:
         if (flags & kErrOverflowListFull) throw Error(MPCD_GB_EDEVICE, "cell overflow list exhausted");
         if (flags & kErrWaitTimeout) throw Error(MPCD_GB_EDEVICE, "device wait timed out");
         if (flags & kErrKeyMismatch) throw Error(MPCD_GB_EDEVICE, "particle found in the wrong cell bucket");
+        if (flags & kErrExtensionFull) throw Error(MPCD_GB_EDEVICE, "cell bucket extension exhausted");
     }
 
     static constexpr int kReduceBlocks = 1024;
@@ -1311,7 +1330,8 @@ private:
     int sms_ = 0, grid_ = 0;
     std::vector<BoxDesc> boxes_;
     uint64_t N_ = 0, cells_ = 0, tiles_ = 0, total_slots_ = 0, walls_ = 0;
-    uint32_t ov_cap_ = 0, pbuf_ = 0;
+    uint32_t ov_cap_ = 0, ext_cap_ = 0, pbuf_ = 0;
+    uint64_t layout_tail_ = 0;   // overflow-list particles of the last layout
     uint32_t max_tile_cells_ = 0, forced_tile_cells_ = 0;   // largest tile of any box; a tile size forced for all
     double fill_ = 1.0;                                      // expected particles per tile = pbuf / fill
     float ext_axis_[13][3];

@@ -197,17 +197,38 @@ __device__ __forceinline__ void push_overflow(const StepArgs& a, uint32_t key, f
 
 // Put one particle (already streamed and shifted for the next collision, in
 // cell `key`) into its bucket, or into the overflow list when the bucket is full.
+// pos.w = kNoExt: a cell the selection does not reach keeps reading its bucket.
 __device__ __forceinline__ void store_particle(const StepArgs& a, const BoxDesc& b, float3 xs, float3 vs, uint32_t id,
                                                uint32_t key, bool active)
 {
     const uint32_t slot = claim_slot(a.out_count, key, active);
     if (!active) return;
-    const float4 xp = make_float4(xs.x, xs.y, xs.z, 0.0f), vp = make_float4(vs.x, vs.y, vs.z, __uint_as_float(id));
-    if (slot < b.cap) {
-        store_slot(a.out_slots + b.slot_base + (uint64_t)(key - b.cell_base) * b.cap + slot, xp, vp);
+    const float4 xp = make_float4(xs.x, xs.y, xs.z, __uint_as_float(kNoExt));
+    const float4 vp = make_float4(vs.x, vs.y, vs.z, __uint_as_float(id));
+    if (slot < b.depth) {
+        store_slot(a.out_slots + b.slot_base + (uint64_t)(key - b.cell_base) * b.depth + slot, xp, vp);
     } else {
         push_overflow(a, key, xp, vp);
     }
+}
+
+// The colliding particles of box-local cell `local` (raw count `raw`): returns
+// their number, with src at the first of them -- the cell's bucket, or, when the
+// cell received more than its depth, the extension slots that
+// overflow_select_kernel filled (offset in pos.w of the first bucket slot).  A
+// cell without an extension (the selection ran out of room, kErrExtensionFull)
+// collides the bucket's depth particles; its list entries stay untaken and skip
+// the collision, so that every particle is still moved exactly once.
+__device__ __forceinline__ uint32_t cell_source(const StepArgs& a, const BoxDesc& b, const Slot* slots,
+                                                uint32_t local, uint32_t raw, const Slot*& src)
+{
+    src = slots + b.slot_base + (uint64_t)local * b.depth;
+    if (raw <= b.depth) return raw;
+    const uint32_t m = min(raw, b.cap);
+    const uint32_t off = __float_as_uint(src->pos.w);
+    if (off > a.ext_cap - m) return b.depth;
+    src = slots + a.total_slots + off;
+    return m;
 }
 
 // ------------------------------------------------------------------ draws
@@ -494,20 +515,22 @@ __device__ __forceinline__ uint32_t fetch_count(const StepArgs& a, uint32_t firs
     return a.in_count[g];
 }
 
-// Overflow particles of step k (they found their bucket full when step k-1
-// scattered them): as in the reference, they skip the collision and keep the
+// Overflow particles of step k past their cell's colliding set (the cap lowest
+// ids of a cell collide; the selection marked the entries it moved to the cell's
+// extension kTakenId): as in the reference, they skip the collision and keep the
 // unshifted position pbc(pbc(x + s) - s) (simulation_functions.cpp:90-93).
 __device__ void overflow_pass(const StepArgs& a, uint64_t step)
 {
     const uint32_t n = min(a.state->ov_count[a.ov_in_slot], a.ov_cap);
     for (uint32_t base = 0; base < n; base += kThreads) {
         const uint32_t q = base + threadIdx.x;
-        const bool active = q < n;
+        const float4 w = q < n ? a.ov_in_vel[q] : make_float4(0, 0, 0, 0);
+        const bool active = q < n && __float_as_uint(w.w) != kTakenId;
         int bi = 0;
         uint32_t id = 0, key = 0;
         float3 x = make_float3(0, 0, 0), v = x, xs = x, vs = x;
         if (active) {
-            const float4 p = a.ov_in_pos[q], w = a.ov_in_vel[q];
+            const float4 p = a.ov_in_pos[q];
             id = __float_as_uint(w.w);
             bi = box_of_particle(a.boxes, a.nboxes, id);
             const BoxDesc& b = a.boxes[bi];
@@ -633,6 +656,7 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
         const bool sign = s.z > 0;
 
         // counts (prefetched) and ghost counts, one group per cell
+        const uint32_t my_raw = next_raw;   // the cell leader's raw count (it stages the cell)
         uint32_t mine = 0, mine_g = 0;
         {
             uint32_t gpart = 0;
@@ -657,7 +681,8 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
             }
             gpart = group_sum(gpart, G);
             if (leader && my_cell < nc) {
-                mine = min(next_raw, b.cap);
+                const Slot* src;
+                mine = cell_source(a, b, a.in_slots, c0 + my_cell, my_raw, src);
                 mine_g = gpart;
                 L.cnt[my_cell] = mine;
                 L.ng[my_cell] = mine_g;
@@ -754,9 +779,10 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                 const uint32_t n = L.cnt[i];
                 const uint32_t o = L.off[i] - pbase, e = L.off[i + 1] - pbase;
                 if (leader && n) {
+                    const Slot* src;
+                    cell_source(a, b, a.in_slots, c0 + i, my_raw, src);
                     fence_proxy_async();
-                    const uint64_t src = b.slot_base + (uint64_t)(c0 + i) * b.cap;
-                    bulk_g2s(s_buf + o, a.in_slots + src, n * 32u, &bar);
+                    bulk_g2s(s_buf + o, src, n * 32u, &bar);
                 }
                 for (uint32_t p = o + my_j; p < e; p += G)   // cell of the entry, kGhostFlag on ghosts
                     s_cell[p] = (uint16_t)(i | (p - o >= n ? kGhostFlag : 0u));
@@ -1111,9 +1137,9 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
                     const uint32_t slot =
                         __shfl_sync(peers[j], base[j], __ffs(peers[j]) - 1) + __popc(peers[j] & lanemask_lt());
                     const float4 xs = s_buf[p].pos, vp = s_buf[p].vel;
-                    const float4 xp = make_float4(xs.x, xs.y, xs.z, 0.0f);
-                    if (slot < b.cap) {
-                        store_slot(a.out_slots + b.slot_base + (uint64_t)(key[j] - b.cell_base) * b.cap + slot, xp, vp);
+                    const float4 xp = make_float4(xs.x, xs.y, xs.z, __uint_as_float(kNoExt));
+                    if (slot < b.depth) {
+                        store_slot(a.out_slots + b.slot_base + (uint64_t)(key[j] - b.cell_base) * b.depth + slot, xp, vp);
                     } else {
                         push_overflow(a, key[j], xp, vp);
                     }
@@ -1221,8 +1247,8 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
     uint2 next = run_entry<SINGLE>(a, run < run_end ? run : a.num_runs);
     uint32_t raw_next = lane < (next.y & 63u) ? a.in_count[next.x + lane] : 0u;   // counts one run ahead
     if (SINGLE && lane < kBatchCells && raw_next)   // the first batch of the first run
-        prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(next.x - b.cell_base + lane) * b.cap,
-                    min(raw_next, b.cap) * (uint32_t)sizeof(Slot));
+        prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(next.x - b.cell_base + lane) * b.depth,
+                    min(raw_next, b.depth) * (uint32_t)sizeof(Slot));
 
     for (; run < run_end; run += warps) {
         const uint2 cur = next;
@@ -1239,11 +1265,16 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
         const bool sign = s.z > 0;
         const uint32_t c = cur.x - b.cell_base + lane;   // box-local cell of this lane
         const bool valid = lane < (cur.y & 63u);
-        const uint32_t cnt = min(raw_next, b.cap);
+        const uint32_t raw = raw_next;
+        // a cell past its bucket depth (rare): its particles lie in the extension area
+        const bool spill = raw > b.depth;
+        const bool run_spill = __any_sync(kFull, spill);
+        const Slot* src_lane;
+        const uint32_t cnt = cell_source(a, b, a.in_slots, c, raw, src_lane);
         if (valid) a.zero_count[cur.x + lane] = 0;   // counts of step k-1: step k+1 fills them
         next = run_entry<SINGLE>(a, run + warps < run_end ? run + warps : a.num_runs);
         raw_next = lane < (next.y & 63u) ? a.in_count[next.x + lane] : 0u;
-        const Slot* const bucket0 = a.in_slots + b.slot_base + (uint64_t)(cur.x - b.cell_base) * b.cap;
+        const Slot* const bucket0 = a.in_slots + b.slot_base + (uint64_t)(cur.x - b.cell_base) * b.depth;
         const uint3 cc = storage_coords(b, valid ? c : 0u);
         bool layer, wall;
         wall_layer(b, cc.z, sign, layer, wall);
@@ -1265,9 +1296,17 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
             sh.gsum[lane][2] = gz;
         }
         const uint32_t m = cnt + ng;   // entries of the cell's collision
-        if (m > 1) {
-            const float3 ax = srd_axis_philox(b, step, ref_index(b, cc));
-            sh.axis[lane] = make_float4(ax.x, ax.y, ax.z, 0.0f);
+        {
+            // rotation axis, and in runs with a spilled cell the cell's extension
+            // offset in .w (kNoExt: the bucket)
+            float4 axw = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kNoExt));
+            if (m > 1) {
+                const float3 ax = srd_axis_philox(b, step, ref_index(b, cc));
+                axw = make_float4(ax.x, ax.y, ax.z, axw.w);
+            }
+            if (spill && src_lane != bucket0 + (uint64_t)lane * b.depth)
+                axw.w = __uint_as_float((uint32_t)(src_lane - a.in_slots - a.total_slots));
+            sh.axis[lane] = axw;
         }
         __syncwarp();
 
@@ -1275,16 +1314,20 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
             // L2 prefetch of the next batch's buckets (after the last batch: the next run's first)
             if (c8 + kBatchCells < kRunCells) {
                 if (lane >= c8 + kBatchCells && lane < c8 + 2 * kBatchCells && cnt)
-                    prefetch_l2(bucket0 + (uint64_t)lane * b.cap, cnt * (uint32_t)sizeof(Slot));
+                    prefetch_l2(bucket0 + (uint64_t)lane * b.depth, min(cnt, b.depth) * (uint32_t)sizeof(Slot));
             } else if (SINGLE && lane < kBatchCells && raw_next) {
-                prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(next.x - b.cell_base + lane) * b.cap,
-                            min(raw_next, b.cap) * (uint32_t)sizeof(Slot));
+                prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(next.x - b.cell_base + lane) * b.depth,
+                            min(raw_next, b.depth) * (uint32_t)sizeof(Slot));
             }
             // exact sums of the batch's real particles: kBatchLanes lanes per cell
             {
                 const uint32_t L = c8 + lane / kBatchLanes, jl = lane % kBatchLanes;
                 const uint32_t cntL = __shfl_sync(kFull, cnt, (int)L), mL = __shfl_sync(kFull, m, (int)L);
-                const Slot* src = bucket0 + (uint64_t)L * b.cap;
+                const Slot* src = bucket0 + (uint64_t)L * b.depth;
+                if (run_spill) {
+                    const uint32_t ew = __float_as_uint(sh.axis[L].w);
+                    if (ew != kNoExt) src = a.in_slots + a.total_slots + ew;
+                }
                 long long sx = 0, sy = 0, sz = 0;
                 unsigned mx = 0;
                 for (uint32_t j = jl; j < cntL; j += 4 * kBatchLanes) {   // four loads in flight per lane
@@ -1353,7 +1396,12 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
                 if (active) {
                     const uint32_t L = c8 + i;
                     float4 xp, vp;
-                    load_slot(bucket0 + (uint64_t)L * b.cap + (t - off), xp, vp);
+                    const Slot* src = bucket0 + (uint64_t)L * b.depth;
+                    if (run_spill) {
+                        const uint32_t ew = __float_as_uint(sh.axis[L].w);
+                        if (ew != kNoExt) src = a.in_slots + a.total_slots + ew;
+                    }
+                    load_slot(src + (t - off), xp, vp);
                     const float4 cd = sh.cell[L];
                     float3 x = make_float3(xp.x, xp.y, xp.z), v = make_float3(vp.x, vp.y, vp.z);
                     if (__float_as_uint(cd.w) > 1) {
@@ -1373,18 +1421,24 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
     }
 }
 
-// Before step k: in every cell that received more particles than its bucket
-// holds (raw count > cap), keep the cap lowest ids in the bucket and move the
-// others to the overflow list, whatever order the claims of step k-1 arrived in:
-// the reference fills each cell's table in particle-index order, and the
-// particles past its depth skip the collision (simulation_functions.cpp:87-93).
-// The thread of a cell's last overflow entry (the head of the cell's chain) walks
-// the raw - cap entries of the chain; each in turn stays in the list or swaps
-// with the bucket's largest id.  Overflow is rare: without any, every thread
-// returns after one load.  Run on the inputs of step k, so a replay of step k
-// finds them already in order.
+// Before step k: every cell that received more particles than its bucket
+// holds (raw count > depth) gets its colliding set -- all raw particles, or the
+// cap lowest ids when raw > cap, whatever order the claims of step k-1 arrived
+// in: the reference fills each cell's table in particle-index order, and the
+// particles past its depth skip the collision (simulation_functions.cpp:87-93) --
+// as min(raw, cap) contiguous slots of the extension area of step k's bucket set.
+// The thread of a cell's last overflow entry (the head of the cell's chain)
+// copies the bucket there, then walks the raw - depth entries of the chain: each
+// fills the next free slot (its list entry is marked taken), or, once cap slots
+// are filled, swaps with the set's largest id if its own id is smaller.  It then
+// records the extension offset in pos.w of the cell's first bucket slot and marks
+// the chain handled, so that a second selection of the same step changes
+// nothing.  Overflow is rare: without any, every thread returns after one load.
+// Run on the inputs of step k, so a replay of step k finds them in place.
+// Block 0 also empties the extension of the other parity (step k+1's: step k-1,
+// its last reader, is past replaying).
 __global__ void __launch_bounds__(kThreads) overflow_select_kernel(const StepArgs a, Slot* in_slots, float4* ov_pos,
-                                                                   float4* ov_vel)
+                                                                   float4* ov_vel, uint32_t* ov_head)
 {
     // Wall ghosts of step k for srd_run_kernel: one thread per wall cell (the two
     // ghost layers of every column) draws the ghost count and the ghosts' summed
@@ -1440,35 +1494,58 @@ __global__ void __launch_bounds__(kThreads) overflow_select_kernel(const StepArg
             a.ghosts[wg] = r;
         }
     }
+    const uint32_t par = (uint32_t)(a.step & 1u);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.state->ext_count[par ^ 1u] = 0;
     const uint32_t n = min(a.state->ov_count[a.ov_in_slot], a.ov_cap);
     for (uint32_t e0 = blockIdx.x * blockDim.x + threadIdx.x; e0 < n; e0 += gridDim.x * blockDim.x) {
+        const uint32_t id0 = __float_as_uint(ov_vel[e0].w);
+        if (id0 == kTakenId) continue;
         const float4 p0 = ov_pos[e0];
-        const int bi = box_of_particle(a.boxes, a.nboxes, __float_as_uint(ov_vel[e0].w));
+        const int bi = box_of_particle(a.boxes, a.nboxes, id0);
         const BoxDesc& b = a.boxes[bi];
         const uint32_t key = b.cell_base + storage_index(b, cell_of_wrapped(b, make_float3(p0.x, p0.y, p0.z)));
-        if (a.ov_head_in[key] != e0) continue;   // not the head of its cell's chain
+        if (ov_head[key] != e0) continue;   // not the head of its cell's chain (or handled)
+        ov_head[key] = kChainDone;
         const uint32_t raw = a.in_count[key];
-        const uint64_t base = b.slot_base + (uint64_t)(key - b.cell_base) * b.cap;
-        uint32_t e = e0;
-        for (uint32_t t = b.cap; t < raw && e < a.ov_cap; ++t) {
+        const uint32_t m = min(raw, b.cap);
+        if (raw <= b.depth) continue;   // (an entry exists only past the depth)
+        Slot* const bucket = in_slots + b.slot_base + (uint64_t)(key - b.cell_base) * b.depth;
+        const uint32_t off = atomicAdd(&a.state->ext_count[par], m);
+        if (off > a.ext_cap - m) {   // no room: the cell keeps its bucket, the step kernels read only that
+            atomicOr(&a.state->error_flags, kErrExtensionFull);
+            bucket->pos.w = __uint_as_float(kNoExt);
+            continue;
+        }
+        Slot* const ext = in_slots + a.total_slots + off;
+        for (uint32_t j = 0; j < b.depth; ++j) ext[j] = bucket[j];
+        uint32_t filled = b.depth, e = e0;
+        for (uint32_t t = b.depth; t < raw && e < a.ov_cap; ++t) {
             const uint32_t before = a.ov_next_in[e];
-            uint32_t jmax = 0, idmax = __float_as_uint(in_slots[base].vel.w);
-            for (uint32_t j = 1; j < b.cap; ++j) {
-                const uint32_t id = __float_as_uint(in_slots[base + j].vel.w);
-                if (id > idmax) {
-                    idmax = id;
-                    jmax = j;
-                }
-            }
             const float4 pe = ov_pos[e], we = ov_vel[e];
-            if (__float_as_uint(we.w) < idmax) {
-                ov_pos[e] = in_slots[base + jmax].pos;
-                ov_vel[e] = in_slots[base + jmax].vel;
-                in_slots[base + jmax].pos = pe;
-                in_slots[base + jmax].vel = we;
+            if (filled < m) {
+                ext[filled].pos = pe;
+                ext[filled].vel = we;
+                ++filled;
+                ov_vel[e].w = __uint_as_float(kTakenId);
+            } else {
+                uint32_t jmax = 0, idmax = __float_as_uint(ext[0].vel.w);
+                for (uint32_t j = 1; j < m; ++j) {
+                    const uint32_t id = __float_as_uint(ext[j].vel.w);
+                    if (id > idmax) {
+                        idmax = id;
+                        jmax = j;
+                    }
+                }
+                if (__float_as_uint(we.w) < idmax) {
+                    ov_pos[e] = ext[jmax].pos;
+                    ov_vel[e] = ext[jmax].vel;
+                    ext[jmax].pos = pe;
+                    ext[jmax].vel = we;
+                }
             }
             e = before;
         }
+        bucket->pos.w = __uint_as_float(off);
     }
 }
 
@@ -1552,7 +1629,8 @@ __global__ void mean_fields_kernel(const SampleAcc* acc, BoxDesc b, double inver
 
 // ------------------------------------------------------------------ compaction
 
-// Decoupled look-back exclusive scan of min(count, cap) over all cells
+// Decoupled look-back exclusive scan of min(count, cap) over all cells (the
+// colliding particles of each cell)
 // (Merrill & Garland, "Single-pass parallel prefix scan with decoupled look-back").
 // status[t]: bits 62-63 flag (1 aggregate, 2 inclusive prefix), low 32 value.
 constexpr int kScanItems = 8;
@@ -1650,8 +1728,9 @@ __global__ void __launch_bounds__(kThreads) compact_kernel(const StepArgs a, con
             if (a.boxes[mid].cell_base <= c) lo = mid; else hi = mid - 1;
         }
         const BoxDesc& b = a.boxes[lo];
-        const uint32_t n = min(count[c], b.cap);
-        const uint64_t slot0 = b.slot_base + (c - b.cell_base) * b.cap;
+        const Slot* src;
+        const uint32_t n = cell_source(a, b, slots, (uint32_t)(c - b.cell_base), count[c], src);
+        const uint64_t slot0 = (uint64_t)(src - slots);
         const uint32_t dst0 = offsets[c];
         const uint32_t ref = ref_index(b, storage_coords(b, (uint32_t)(c - b.cell_base)));
         for (uint32_t q = 0; q < n; ++q) {
@@ -1674,26 +1753,31 @@ __global__ void __launch_bounds__(kThreads) compact_kernel(const StepArgs a, con
     }
 }
 
-__global__ void compact_overflow_kernel(const BoxDesc* boxes, int nboxes, uint64_t step, const float4* ov_pos,
+// The overflow list's particles that do not collide (entries not taken into an
+// extension), after the cells' particles in any order (the host orders them by
+// cell and id); *placed counts them.  slot = total_slots + ext_cap + entry.
+__global__ void compact_overflow_kernel(const BoxDesc* boxes, int nboxes, const float4* ov_pos,
                                         const float4* ov_vel, const DeviceState* st, unsigned parity, uint32_t ov_cap,
                                         const uint32_t* offsets, uint64_t cells, uint64_t n_total,
-                                        uint64_t total_slots, uint32_t* out_cell, uint32_t* out_slot,
-                                        uint32_t* out_prev, uint32_t* out_id)
+                                        uint64_t list_slot0, unsigned int* placed, uint32_t* out_cell,
+                                        uint32_t* out_slot, uint32_t* out_prev, uint32_t* out_id)
 {
     const uint32_t n = min(st->ov_count[parity], ov_cap);
     const uint32_t base = offsets[cells];
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        const uint64_t d = (uint64_t)base + q;
-        if (d >= n_total) break;
+        const uint32_t id = __float_as_uint(ov_vel[q].w);
+        if (id == kTakenId) continue;
+        const uint64_t d = (uint64_t)base + atomicAdd(placed, 1u);
+        if (d >= n_total) continue;
         if (out_cell) {   // the cell the (already streamed) particle is keyed to
-            const float4 p = ov_pos[q], w = ov_vel[q];
-            const int bi = box_of_particle(boxes, nboxes, __float_as_uint(w.w));
+            const float4 p = ov_pos[q];
+            const int bi = box_of_particle(boxes, nboxes, id);
             const BoxDesc& b = boxes[bi];
             out_cell[d] = b.cell_base + ref_index(b, cell_of(b, make_float3(p.x, p.y, p.z)));
         }
-        if (out_slot) out_slot[d] = (uint32_t)(total_slots + q);
-        if (out_prev) out_prev[d] = __float_as_uint(ov_vel[q].w);
-        if (out_id) out_id[d] = __float_as_uint(ov_vel[q].w);
+        if (out_slot) out_slot[d] = (uint32_t)(list_slot0 + q);
+        if (out_prev) out_prev[d] = id;
+        if (out_id) out_id[d] = id;
     }
 }
 
@@ -2004,10 +2088,10 @@ cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel
     return cudaGetLastError();
 }
 
-cudaError_t launch_overflow_select(const StepArgs& a, Slot* in_slots, float4* ov_pos, float4* ov_vel, int grid,
-                                   cudaStream_t st)
+cudaError_t launch_overflow_select(const StepArgs& a, Slot* in_slots, float4* ov_pos, float4* ov_vel,
+                                   uint32_t* ov_head, int grid, cudaStream_t st)
 {
-    overflow_select_kernel<<<grid, kThreads, 0, st>>>(a, in_slots, ov_pos, ov_vel);
+    overflow_select_kernel<<<grid, kThreads, 0, st>>>(a, in_slots, ov_pos, ov_vel, ov_head);
     return cudaGetLastError();
 }
 
@@ -2041,9 +2125,11 @@ cudaError_t launch_layout(const StepArgs& a, const uint32_t* count, const Slot* 
                                                       a.state);
     compact_kernel<<<grid, kThreads, 0, st>>>(a, count, slots, offsets, cells, n_total, out_cell, out_slot,
                                               out_prev, out_id);
-    compact_overflow_kernel<<<8, kThreads, 0, st>>>(a.boxes, a.nboxes, a.step, ov_pos, ov_vel, a.state, parity,
-                                                    a.ov_cap, offsets, cells, n_total, a.total_slots, out_cell,
-                                                    out_slot, out_prev, out_id);
+    e = cudaMemsetAsync(tile_counter, 0, sizeof(unsigned int), st);   // now the count of placed list entries
+    if (e != cudaSuccess) return e;
+    compact_overflow_kernel<<<8, kThreads, 0, st>>>(a.boxes, a.nboxes, ov_pos, ov_vel, a.state, parity, a.ov_cap,
+                                                    offsets, cells, n_total, a.total_slots + a.ext_cap, tile_counter,
+                                                    out_cell, out_slot, out_prev, out_id);
     return cudaGetLastError();
 }
 

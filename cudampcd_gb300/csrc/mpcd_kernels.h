@@ -26,11 +26,12 @@ cudaError_t launch_advance(DeviceState* state, unsigned steps, cudaStream_t st);
 // Key dense clean particles for step a.step + 1 and scatter them into a.out_*.
 cudaError_t launch_scatter(const StepArgs& a, const float* pos, const float* vel, uint64_t n_total, int grid,
                            cudaStream_t st);
-// Before a step (not a replay): the particles the reference keeps in each overflowing
-// cell into its bucket, the others into the overflow list (in_* / ov_*: the step's
-// input buckets and list, a.in_count, a.ov_head_in and a.ov_next_in its chains).
+// Before a step (not a replay): the particles the reference keeps in each cell past
+// its bucket depth into the extension area after the buckets, the others left in
+// the overflow list (in_* / ov_*: the step's input buckets and list, a.in_count,
+// ov_head and a.ov_next_in its chains).  A second call for the same step does nothing.
 cudaError_t launch_overflow_select(const StepArgs& a, Slot* in_slots, float4* ov_pos, float4* ov_vel,
-                                   int grid, cudaStream_t st);
+                                   uint32_t* ov_head, int grid, cudaStream_t st);
 // Lab-grid sample of one step into the FP64 running sums (and clear the step sums).
 cudaError_t launch_sample_finalize(float4* samp, SampleAcc* acc, uint64_t cells, int snapshot, int grid,
                                    cudaStream_t st, uint32_t* lab_count = nullptr);
@@ -47,9 +48,10 @@ cudaError_t launch_adjoint_step(const BoxDesc& b, uint64_t step, uint64_t sample
                                 const float* dU, float4* cellsum, double* gsum, int grid, cudaStream_t st);
 cudaError_t launch_adjoint_finish(uint32_t n, const float* lam, const uint32_t* b0, float* out, int grid,
                                   cudaStream_t st);
-// Layout dump: cells in storage order, stable order within a cell (decoupled
-// look-back scan of the counts, then one thread per cell), then the overflow
-// list.  offsets: cells + 1 entries.
+// Layout dump, after the step's overflow selection: cells in storage order, stable
+// order within a cell (decoupled look-back scan of the counts, then one thread per
+// cell), then the overflow list's particles that do not collide, in any order;
+// their number lands in *tile_counter.  offsets: cells + 1 entries.
 cudaError_t launch_layout(const StepArgs& a, const uint32_t* count, const Slot* slots,
                           uint32_t* offsets, uint64_t cells, uint64_t n_total, unsigned long long* status,
                           unsigned int* tile_counter, const float4* ov_pos, const float4* ov_vel, unsigned parity,

@@ -1,8 +1,15 @@
 // Host/device data structures of the GB300 MPCD step.
 //
-// Particles live in per-cell buckets: cell c of a box owns `cap` slots
-// (cap = 4n, the depth of the reference's cell table, backend_context.cu:24) of
-// 32 bytes each, one DRAM sector: pos = (x, y, z, 0), vel = (vx, vy, vz, id).
+// Particles live in per-cell buckets: cell c of a box owns `depth` slots of 32
+// bytes each, one DRAM sector: pos = (x, y, z, 0), vel = (vx, vy, vz, id).  The
+// reference's cell table is 4n deep (cap, backend_context.cu:24): up to cap
+// particles of a cell collide.  depth = min(cap, n + ceil(4 sqrt(n)) + 2) holds
+// all but about one cell in 10^4..10^5 at equilibrium; the particles of a cell
+// past its depth go to the overflow list, and the step's prologue
+// (overflow_select_kernel) copies such a cell's colliding set -- its cap lowest
+// ids -- into a contiguous extension area after the buckets, records the
+// extension offset in pos.w of the cell's first bucket slot, and marks the list
+// entries it took as taken (id kTakenId).
 // A bucket set for step k holds every particle as it enters the collision of
 // step k: streamed and shifted by the grid shift of step k, in the bucket of the
 // cell it then occupies (the reference's translate output, simulation_functions.cpp:38-103).
@@ -43,7 +50,7 @@ struct BoxDesc {
     float R2;              // channel radius^2, (Lz - 2)^2 / 4
     float cos_a, sin_a;    // SRD rotation by 120 degrees (host libm, as the reference)
     uint32_t n;            // particles per cell
-    uint32_t cap;          // bucket depth, 4n
+    uint32_t cap;          // colliding particles per cell at most, 4n
     uint32_t C;            // cells
     uint32_t N;            // particles
     uint32_t cell_base;    // first global cell of this box
@@ -56,7 +63,7 @@ struct BoxDesc {
     uint32_t seed_lo, seed_hi;
     uint64_t wall_base;    // first wall-ghost entry of this box (2 per column, with walls in z)
     uint32_t run_batch;    // srd_run_kernel: cells summed and finished together (4, 8 or 16)
-    uint32_t unused;
+    uint32_t depth;        // bucket slots per cell (<= cap)
 };
 
 // The step kernel copies a box descriptor into shared memory 16 bytes per thread.
@@ -94,13 +101,19 @@ struct DeviceState {
     unsigned int inject_valid[kMaxInjectedShifts];
     unsigned long long step_base;        // graph replays: absolute step of the replay's first step
     double wall_impulse[2];              // pressure estimator: outward impulse on the z walls {bottom, top}
+    unsigned int ext_count[2];           // bucket extension fill, by step parity
 };
 
 enum : unsigned int {
     kErrOverflowListFull = 1u,
     kErrWaitTimeout = 2u,
     kErrKeyMismatch = 4u,
+    kErrExtensionFull = 8u,
 };
+
+constexpr uint32_t kTakenId = 0xFFFFFFFFu;    // overflow-list entry moved to its cell's extension
+constexpr uint32_t kChainDone = 0xFFFFFFFFu;  // chain head of a cell the selection has handled
+constexpr uint32_t kNoExt = 0xFFFFFFFFu;      // extension offset of a cell whose extension failed
 
 // Injected per-cell draws (reference cell order of box 0), test hook.
 struct DrawTables {
@@ -120,7 +133,8 @@ struct StepArgs {
     uint32_t boxes_tile_cells;    // the largest tile (cells) of any box of the launch
     const TileEntry* tile_info;   // ensembles: one entry per tile
     uint32_t num_tiles;
-    uint64_t total_slots;
+    uint64_t total_slots;         // bucket slots of all boxes; the extension area follows them
+    uint32_t ext_cap;             // extension slots (>= every box's cap)
     uint64_t step;                // k: this launch completes step k (step_base: k - *step_base)
     const unsigned long long* step_base;   // non-null in graph replays: k = *step_base + step
     // buckets holding the particles entering collision k (streamed, shifted)
@@ -142,7 +156,8 @@ struct StepArgs {
     // parity and are never cleared: a step reads the head of a cell only when the
     // cell's count exceeds its depth, so the previous step's claims wrote it, and
     // it follows exactly count - depth links (the last one would lead to older
-    // entries).
+    // entries).  The selection sets a handled cell's head to kChainDone, so that a
+    // second selection of the same step (the layout dump runs one) changes nothing.
     const uint32_t* ov_head_in;
     uint32_t* ov_head_out;
     const uint32_t* ov_next_in;   // by entry of ov_in

@@ -130,12 +130,16 @@ int32_t mpcd_gb_get_shift(mpcd_gb_handle *h, uint64_t step, float shift[3]);
 
 /* Layout of the current cell buckets -- the counting sort by cell -- one entry
  * per particle in layout order: cells in storage order (z fastest, then x, then
- * y), within a cell ascending particle id (the stable sort of the id-ordered
- * particle array by cell), then the particles waiting in the overflow list
- * ordered by (cell, id).  cell = reference cell index x + Lx*(y + Ly*z) the
- * particle is keyed to, slot = its sparse slot id, id = particle id.  counts: C
- * entries (reference cell order), the number of particles each cell received,
- * overflow included (the reference's uniform_counter).  Any pointer may be NULL. */
+ * y), within a cell its colliding particles (up to 4n) by ascending particle id
+ * (the stable sort of the id-ordered particle array by cell), then the particles
+ * past a cell's 4n, which skip the collision, ordered by (cell, id).  cell =
+ * reference cell index x + Lx*(y + Ly*z) the particle is keyed to, id = particle
+ * id, slot = where the handle stores it: a bucket slot, an extension slot
+ * (bucket slots + offset) or an overflow-list entry (bucket and extension slots +
+ * entry); within a cell, slots are numbered in id order.  counts: C entries
+ * (reference cell order), the number of particles each cell received, overflow
+ * included (the reference's uniform_counter).  Runs the next step's overflow
+ * selection (which that step then finds done).  Any pointer may be NULL. */
 int32_t mpcd_gb_dump_layout(mpcd_gb_handle *h, uint32_t *cell, uint32_t *slot, uint32_t *id, uint32_t *counts);
 
 /* Injected draws for the next step (the oracle's recorded tables, reference
@@ -146,8 +150,11 @@ int32_t mpcd_gb_inject_draws(mpcd_gb_handle *h, uint32_t gmax, uint32_t pmax, co
                              const float *ghost_pos, const float *ghost_vel, const float *axis,
                              const float *gate_u, const float *gauss);
 
-/* Device-side counters: [0] particles that overflowed a cell bucket (all time),
- * [1] error flags (bit 0 overflow list full, bit 1 wait timeout, bit 2 key mismatch). */
+/* Device-side counters: [0] particles that found their cell's bucket full (all time;
+ * buckets are min(4n, n + ceil(4 sqrt(n)) + 2) deep, so this counts more than the
+ * reference's overflow past 4n),
+ * [1] error flags (bit 0 overflow list full, bit 1 wait timeout, bit 2 key mismatch,
+ * bit 3 bucket extension full). */
 int32_t mpcd_gb_counters(mpcd_gb_handle *h, uint64_t out[2]);
 
 /* ---- snapshots: checkpoint and resume (the reference's writeBackupFile is a TODO,

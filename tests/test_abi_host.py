@@ -49,7 +49,7 @@ def test_abi_version_matches_header():
     (dict(drag=float("inf")), "drag"),
     (dict(n=500), "n above 409"),
     (dict(L=(2048, 2048, 512), n=1), "too many cells"),
-    (dict(L=(1024, 1024, 110), n=10), "slot space"),
+    (dict(L=(1024, 1024, 200), n=10), "slot space"),
 ])
 def test_create_rejects_invalid_parameters_before_touching_the_device(kw, message):
     rc, err, h = _create(**kw)
