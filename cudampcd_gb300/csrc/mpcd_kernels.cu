@@ -1265,16 +1265,15 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
         const bool sign = s.z > 0;
         const uint32_t c = cur.x - b.cell_base + lane;   // box-local cell of this lane
         const bool valid = lane < (cur.y & 63u);
-        const uint32_t raw = raw_next;
-        // a cell past its bucket depth (rare): its particles lie in the extension area
-        const bool spill = raw > b.depth;
-        const bool run_spill = __any_sync(kFull, spill);
+        // the lane's cell: its colliding particles and the slot of the first (its
+        // bucket, or for a cell past its depth its extension; below 2^32, which the
+        // engine checks)
         const Slot* src_lane;
-        const uint32_t cnt = cell_source(a, b, a.in_slots, c, raw, src_lane);
+        const uint32_t cnt = cell_source(a, b, a.in_slots, c, raw_next, src_lane);
+        const uint32_t src_slot = (uint32_t)(src_lane - a.in_slots);
         if (valid) a.zero_count[cur.x + lane] = 0;   // counts of step k-1: step k+1 fills them
         next = run_entry<SINGLE>(a, run + warps < run_end ? run + warps : a.num_runs);
         raw_next = lane < (next.y & 63u) ? a.in_count[next.x + lane] : 0u;
-        const Slot* const bucket0 = a.in_slots + b.slot_base + (uint64_t)(cur.x - b.cell_base) * b.depth;
         const uint3 cc = storage_coords(b, valid ? c : 0u);
         bool layer, wall;
         wall_layer(b, cc.z, sign, layer, wall);
@@ -1296,17 +1295,9 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
             sh.gsum[lane][2] = gz;
         }
         const uint32_t m = cnt + ng;   // entries of the cell's collision
-        {
-            // rotation axis, and in runs with a spilled cell the cell's extension
-            // offset in .w (kNoExt: the bucket)
-            float4 axw = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kNoExt));
-            if (m > 1) {
-                const float3 ax = srd_axis_philox(b, step, ref_index(b, cc));
-                axw = make_float4(ax.x, ax.y, ax.z, axw.w);
-            }
-            if (spill && src_lane != bucket0 + (uint64_t)lane * b.depth)
-                axw.w = __uint_as_float((uint32_t)(src_lane - a.in_slots - a.total_slots));
-            sh.axis[lane] = axw;
+        if (m > 1) {
+            const float3 ax = srd_axis_philox(b, step, ref_index(b, cc));
+            sh.axis[lane] = make_float4(ax.x, ax.y, ax.z, 0.0f);
         }
         __syncwarp();
 
@@ -1314,7 +1305,7 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
             // L2 prefetch of the next batch's buckets (after the last batch: the next run's first)
             if (c8 + kBatchCells < kRunCells) {
                 if (lane >= c8 + kBatchCells && lane < c8 + 2 * kBatchCells && cnt)
-                    prefetch_l2(bucket0 + (uint64_t)lane * b.depth, min(cnt, b.depth) * (uint32_t)sizeof(Slot));
+                    prefetch_l2(a.in_slots + src_slot, cnt * (uint32_t)sizeof(Slot));
             } else if (SINGLE && lane < kBatchCells && raw_next) {
                 prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(next.x - b.cell_base + lane) * b.depth,
                             min(raw_next, b.depth) * (uint32_t)sizeof(Slot));
@@ -1323,11 +1314,7 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
             {
                 const uint32_t L = c8 + lane / kBatchLanes, jl = lane % kBatchLanes;
                 const uint32_t cntL = __shfl_sync(kFull, cnt, (int)L), mL = __shfl_sync(kFull, m, (int)L);
-                const Slot* src = bucket0 + (uint64_t)L * b.depth;
-                if (run_spill) {
-                    const uint32_t ew = __float_as_uint(sh.axis[L].w);
-                    if (ew != kNoExt) src = a.in_slots + a.total_slots + ew;
-                }
+                const Slot* src = a.in_slots + __shfl_sync(kFull, src_slot, (int)L);
                 long long sx = 0, sy = 0, sz = 0;
                 unsigned mx = 0;
                 for (uint32_t j = jl; j < cntL; j += 4 * kBatchLanes) {   // four loads in flight per lane
@@ -1373,6 +1360,7 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
             // cell i when end_{i-1} <= t < end_i (ends: inclusive prefix of the counts,
             // held by lanes 0..7)
             const uint32_t bc = __shfl_sync(kFull, cnt, (int)(c8 + (lane & (kBatchCells - 1))));
+            const uint32_t bslot = __shfl_sync(kFull, src_slot, (int)(c8 + (lane & (kBatchCells - 1))));
             uint32_t bi = lane < kBatchCells ? bc : 0u;
 #pragma unroll
             for (int d = 1; d < (int)kBatchCells; d <<= 1) {
@@ -1380,28 +1368,27 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
                 if ((int)lane >= d) bi += t;
             }
             const uint32_t btot = __shfl_sync(kFull, bi, kBatchCells - 1);
+            // lane i < BATCH: slot of batch cell i's first particle minus the batch
+            // particles before it (modulo 2^32), so that particle t of cell i lies in slot
+            // rel + t
+            const uint32_t rel = bslot - (bi - (lane < kBatchCells ? bc : 0u));
             __syncwarp();   // the batch's means are written
             for (uint32_t e0 = 0; e0 < btot; e0 += 32) {
                 const uint32_t t = e0 + lane;
                 const bool active = t < btot;
                 // batch cell i of particle t: the number of cells that end at or before t
-                // (binary search over the ends), and its first particle
+                // (binary search over the ends), and its slot
                 uint32_t i = 0;
 #pragma unroll
                 for (uint32_t half = kBatchCells / 2; half; half >>= 1)
                     i += t >= __shfl_sync(kFull, bi, (int)(i + half - 1)) ? half : 0u;
-                const uint32_t off = __shfl_sync(kFull, bi, (int)((i + kBatchCells - 1) & (kBatchCells - 1))) & (i ? ~0u : 0u);
+                const uint32_t slot = __shfl_sync(kFull, rel, (int)i) + t;
                 uint32_t key = 0, id = 0;
                 float3 xn = make_float3(0, 0, 0), vn = xn;
                 if (active) {
                     const uint32_t L = c8 + i;
                     float4 xp, vp;
-                    const Slot* src = bucket0 + (uint64_t)L * b.depth;
-                    if (run_spill) {
-                        const uint32_t ew = __float_as_uint(sh.axis[L].w);
-                        if (ew != kNoExt) src = a.in_slots + a.total_slots + ew;
-                    }
-                    load_slot(src + (t - off), xp, vp);
+                    load_slot(a.in_slots + slot, xp, vp);
                     const float4 cd = sh.cell[L];
                     float3 x = make_float3(xp.x, xp.y, xp.z), v = make_float3(vp.x, vp.y, vp.z);
                     if (__float_as_uint(cd.w) > 1) {
