@@ -1301,17 +1301,40 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
         }
         __syncwarp();
 
-        for (uint32_t c8 = 0; c8 < kRunCells; c8 += kBatchCells) {
-            // L2 prefetch of the next batch's buckets (after the last batch: the next run's first)
-            if (c8 + kBatchCells < kRunCells) {
-                if (lane >= c8 + kBatchCells && lane < c8 + 2 * kBatchCells && cnt)
-                    prefetch_l2(a.in_slots + src_slot, cnt * (uint32_t)sizeof(Slot));
-            } else if (SINGLE && lane < kBatchCells && raw_next) {
-                prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(next.x - b.cell_base + lane) * b.depth,
-                            min(raw_next, b.depth) * (uint32_t)sizeof(Slot));
-            }
-            // exact sums of the batch's real particles: kBatchLanes lanes per cell
-            {
+        // the run's particles in order: cell c holds run particles [incl_c - cnt_c,
+        // incl_c) (incl: inclusive prefix of the counts over the run's lanes), and run
+        // particle t of cell c lies in slot rel_c + t (modulo 2^32)
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(kFull, incl, d);
+            if ((int)lane >= d) incl += t;
+        }
+        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        const uint32_t rel = src_slot - (incl - cnt);
+        uint32_t summed = 0;           // cells [0, summed) have their means in sh.cell
+        bool next_prefetched = false;  // the next run's first batch was asked of L2
+        // 32 particles at a time, across batch boundaries
+        for (uint32_t g0 = 0; g0 < total; g0 += 32) {
+            const uint32_t t = g0 + lane;
+            const bool active = t < total;
+            // cells of the group's first and last particles: the cells that end at or before them
+            const uint32_t lo = __popc(__ballot_sync(kFull, incl <= g0));
+            const uint32_t hi = __popc(__ballot_sync(kFull, incl <= min(g0 + 31u, total - 1u)));
+            // exact sums and means of every cell up to hi, a batch of BATCH cells at a
+            // time (kBatchLanes lanes per cell); each batch asks L2 for the next one's buckets
+            while (summed <= hi) {
+                const uint32_t c8 = summed;
+                summed += kBatchCells;
+                if (c8 + kBatchCells < kRunCells) {
+                    if (lane >= c8 + kBatchCells && lane < c8 + 2 * kBatchCells && cnt)
+                        prefetch_l2(a.in_slots + src_slot, cnt * (uint32_t)sizeof(Slot));
+                } else {
+                    next_prefetched = true;
+                    if (SINGLE && lane < kBatchCells && raw_next)
+                        prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(next.x - b.cell_base + lane) * b.depth,
+                                    min(raw_next, b.depth) * (uint32_t)sizeof(Slot));
+                }
                 const uint32_t L = c8 + lane / kBatchLanes, jl = lane % kBatchLanes;
                 const uint32_t cntL = __shfl_sync(kFull, cnt, (int)L), mL = __shfl_sync(kFull, m, (int)L);
                 const Slot* src = a.in_slots + __shfl_sync(kFull, src_slot, (int)L);
@@ -1356,54 +1379,47 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
                     sh.cell[L] = make_float4(mean.x, mean.y, mean.z, __uint_as_float(mL));
                 }
             }
-            // the batch's particles in order, 32 at a time: particle t lies in batch
-            // cell i when end_{i-1} <= t < end_i (ends: inclusive prefix of the counts,
-            // held by lanes 0..7)
-            const uint32_t bc = __shfl_sync(kFull, cnt, (int)(c8 + (lane & (kBatchCells - 1))));
-            const uint32_t bslot = __shfl_sync(kFull, src_slot, (int)(c8 + (lane & (kBatchCells - 1))));
-            uint32_t bi = lane < kBatchCells ? bc : 0u;
+            __syncwarp();   // the means are written
+            // cell i of particle t: the first cell that ends after t -- within [lo, lo + W)
+            // when the group spans at most W cells (W = 4, or 8 with 16-cell batches), else
+            // over the run (incl of lane 31 is the run's total, beyond every active t)
+            constexpr uint32_t kWindow = BATCH == 16 ? 8u : 4u;
+            uint32_t i;
+            if (hi - lo < kWindow) {
+                i = lo;
 #pragma unroll
-            for (int d = 1; d < (int)kBatchCells; d <<= 1) {
-                const uint32_t t = __shfl_up_sync(kFull, bi, d);
-                if ((int)lane >= d) bi += t;
+                for (uint32_t half = kWindow / 2; half; half >>= 1)
+                    i += t >= __shfl_sync(kFull, incl, (int)min(i + half - 1u, 31u)) ? half : 0u;
+            } else {
+                i = 0;
+#pragma unroll
+                for (uint32_t half = 16; half; half >>= 1)
+                    i += t >= __shfl_sync(kFull, incl, (int)(i + half - 1)) ? half : 0u;
             }
-            const uint32_t btot = __shfl_sync(kFull, bi, kBatchCells - 1);
-            // lane i < BATCH: slot of batch cell i's first particle minus the batch
-            // particles before it (modulo 2^32), so that particle t of cell i lies in slot
-            // rel + t
-            const uint32_t rel = bslot - (bi - (lane < kBatchCells ? bc : 0u));
-            __syncwarp();   // the batch's means are written
-            for (uint32_t e0 = 0; e0 < btot; e0 += 32) {
-                const uint32_t t = e0 + lane;
-                const bool active = t < btot;
-                // batch cell i of particle t: the number of cells that end at or before t
-                // (binary search over the ends), and its slot
-                uint32_t i = 0;
-#pragma unroll
-                for (uint32_t half = kBatchCells / 2; half; half >>= 1)
-                    i += t >= __shfl_sync(kFull, bi, (int)(i + half - 1)) ? half : 0u;
-                const uint32_t slot = __shfl_sync(kFull, rel, (int)i) + t;
-                uint32_t key = 0, id = 0;
-                float3 xn = make_float3(0, 0, 0), vn = xn;
-                if (active) {
-                    const uint32_t L = c8 + i;
-                    float4 xp, vp;
-                    load_slot(a.in_slots + slot, xp, vp);
-                    const float4 cd = sh.cell[L];
-                    float3 x = make_float3(xp.x, xp.y, xp.z), v = make_float3(vp.x, vp.y, vp.z);
-                    if (__float_as_uint(cd.w) > 1) {
-                        const float4 ax = sh.axis[L];
-                        srd_collide(b, s, make_float3(cd.x, cd.y, cd.z), make_float3(ax.x, ax.y, ax.z), x, v);
-                    }
-                    vn = v;
-                    xn = stream_shift(b, x, vn, sn);
-                    key = b.cell_base + storage_index(b, cell_of_wrapped(b, xn));
-                    id = __float_as_uint(vp.w);
-                    if (SAMPLE) sample_add(a.samp, b.cell_base + storage_index(b, cell_of_wrapped(b, x)), v, true);
+            const uint32_t slot = __shfl_sync(kFull, rel, (int)(i & 31u)) + t;
+            uint32_t key = 0, id = 0;
+            float3 xn = make_float3(0, 0, 0), vn = xn;
+            if (active) {
+                float4 xp, vp;
+                load_slot(a.in_slots + slot, xp, vp);
+                const float4 cd = sh.cell[i];
+                float3 x = make_float3(xp.x, xp.y, xp.z), v = make_float3(vp.x, vp.y, vp.z);
+                if (__float_as_uint(cd.w) > 1) {
+                    const float4 ax = sh.axis[i];
+                    srd_collide(b, s, make_float3(cd.x, cd.y, cd.z), make_float3(ax.x, ax.y, ax.z), x, v);
                 }
-                store_particle(a, b, xn, vn, id, key, active);
+                vn = v;
+                xn = stream_shift(b, x, vn, sn);
+                key = b.cell_base + storage_index(b, cell_of_wrapped(b, xn));
+                id = __float_as_uint(vp.w);
+                if (SAMPLE) sample_add(a.samp, b.cell_base + storage_index(b, cell_of_wrapped(b, x)), v, true);
             }
+            store_particle(a, b, xn, vn, id, key, active);
         }
+        // a run whose last cells are empty: the next run's first batch
+        if (SINGLE && !next_prefetched && lane < kBatchCells && raw_next)
+            prefetch_l2(a.in_slots + b.slot_base + (uint64_t)(next.x - b.cell_base + lane) * b.depth,
+                        min(raw_next, b.depth) * (uint32_t)sizeof(Slot));
         __syncwarp();   // the next run rewrites this warp's shared arrays
     }
 }
