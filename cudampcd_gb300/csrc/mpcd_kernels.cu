@@ -1167,22 +1167,21 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
 // CTA-wide barrier and no staging: each warp works alone on its runs with 1.5
 // KB of shared memory of its own, and reads the particles straight from their
 // buckets (a cell's bucket is contiguous).  Per run:
-//   per cell (its lane): count, wall ghosts (drawn by the step's prologue),
-//   rotation axis;
-//   then batches of 4, 8 or 16 cells (about 80 particles): exact velocity sums of
-//   the batch's particles (32 / batch lanes per cell, four loads in flight each),
-//   and per particle, 32
-//   consecutive particles of the batch at a time (their slots still in L1 from
-//   the sums): the collision, unshift, drag, lab-grid sample, streaming of step
+//   per cell (its lane): count, where its particles lie, wall ghosts (drawn by
+//   the step's prologue), rotation axis; a prefix of the counts over the run;
+//   then the run's particles, 32 consecutive ones at a time across cell and batch
+//   boundaries: the collision, unshift, drag, lab-grid sample, streaming of step
 //   k+1 and its cell, the slot claim (warp-aggregated) and one 256-bit store.
-//   Each batch asks L2 for the next batch's buckets.
+//   Before a group, the cells it reaches get their exact velocity sums and means,
+//   a batch of 4, 8 or 16 cells (about 80 particles) at a time with 32 / batch
+//   lanes per cell and four loads in flight each, so that the group's slots are
+//   still in L1 from the sums.  Each batch asks L2 for the next batch's buckets.
 // The arithmetic is step_kernel's (the same helpers), so a replay of this step
 // by step_kernel (the getters) reproduces it bit for bit.
 
 constexpr uint32_t kRunCells = 32;
-// Cells summed and finished together: BATCH = 4, 8 or 16, about 80 particles per
-// batch (the engine picks it from n: a box's run_batch); 32 / BATCH lanes per cell in
-// the sums.
+// Cells summed together: BATCH = 4, 8 or 16, about 80 particles per batch (the
+// engine picks it from n: a box's run_batch); 32 / BATCH lanes per cell in the sums.
 constexpr int kRunWarps = kThreads / 32;
 constexpr uint32_t kRunMaxN = 64;                     // densities this kernel takes
 
