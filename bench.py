@@ -287,10 +287,12 @@ def cpu_baseline_block(warmup: int, steps: int):
     r = reference_cpu_rate(cores, warmup, steps)
     if r is not None:
         rate, n = r
+        single = reference_cpu_rate(1, warmup, steps)   # the same slab in one process, alone on the host
         return {"value": rate, "unit": UNIT, "cores": cores, "kind": "reference", "cpu": cpu_model(),
                 "sample": f"{cores} processes (one per core; the reference CPU backend is single-threaded), "
                           f"each one slab of the workload, {slab} ({n} particles), pympcd.Simulation(params, "
-                          f"'cpu') of the unchanged reference build; {warmup} warm-up + {steps} timed steps"}
+                          f"'cpu') of the unchanged reference build; {warmup} warm-up + {steps} timed steps",
+                "single_core": {"value": single[0] if single else None, "unit": UNIT, "cores": 1}}
     threads = min(cores, 16)
     rate, n = cpu_rate(threads, warmup, steps)
     return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "cpu": cpu_model(),

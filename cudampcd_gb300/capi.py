@@ -71,6 +71,8 @@ def lib() -> C.CDLL:
         L.mpcd_gb_inject_draws.argtypes = [H, C.c_uint32, C.c_uint32] + [C.c_void_p] * 6
         L.mpcd_gb_counters.argtypes = [H, u64p]
         L.mpcd_gb_cell_offsets_noalloc.argtypes = [H, C.c_void_p, C.c_uint64]
+        L.mpcd_gb_device_allocations.argtypes = []
+        L.mpcd_gb_device_allocations.restype = C.c_uint64
         L.mpcd_gb_ensemble_create.argtypes = [C.c_void_p, C.c_int32, C.POINTER(H)]
         L.mpcd_gb_num_boxes.argtypes = [H]
         L.mpcd_gb_box_range.argtypes = [H, C.c_int32, u64p]
@@ -91,6 +93,11 @@ def lib() -> C.CDLL:
 
 class GbError(RuntimeError):
     pass
+
+
+def device_allocations() -> int:
+    """Device allocations the library has made in this process (all handles)."""
+    return int(lib().mpcd_gb_device_allocations())
 
 
 def make_params(L=(10, 10, 10), periodic=(1, 1, 1), n=10, dt=0.02, drag=0.0, temperature=1.0, algorithm=0,

@@ -7,6 +7,7 @@
 // except the getters, the sample read-out and the error check at the end of
 // step()/step_and_sample().
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
@@ -52,6 +53,9 @@ void shift_host(const BoxDesc& b, uint64_t step, float out[3])
     for (int i = 0; i < 3; ++i) out[i] = (float)(c[i] >> 8) * 0x1p-24f - 0.5f;
 }
 
+// Device allocations the library has made in this process (mpcd_gb_device_allocations).
+std::atomic<unsigned long long> g_device_allocations{0};
+
 struct DeviceBuffer {
     void* p = nullptr;
     size_t bytes = 0;
@@ -67,6 +71,7 @@ struct DeviceBuffer {
         release();
         if (n == 0) return cudaSuccess;
         cudaError_t e = cudaMalloc(&p, n);
+        g_device_allocations.fetch_add(1, std::memory_order_relaxed);
         if (e == cudaSuccess) bytes = n;
         else p = nullptr;
         return e;
@@ -1612,6 +1617,8 @@ int32_t mpcd_gb_autotune(mpcd_gb_handle* h, int32_t steps_per_candidate, uint32_
     if (!out) return MPCD_GB_EINVAL;
     return guarded(h, [&](mpcd_gb::Engine& e) { e.autotune(steps_per_candidate, out); });
 }
+
+uint64_t mpcd_gb_device_allocations(void) { return mpcd_gb::g_device_allocations.load(); }
 
 int32_t mpcd_gb_cell_offsets_noalloc(mpcd_gb_handle* h, uint32_t* d_offsets, uint64_t n_offsets)
 {

@@ -242,6 +242,12 @@ int32_t mpcd_gb_profile_backward(mpcd_gb_handle *h, const float *d_grad_profile,
 int32_t mpcd_gb_profile_tape(mpcd_gb_handle *h, uint32_t *key, uint32_t *lab, uint32_t *ncell, uint32_t *lab_count,
                              uint32_t *bounce0);
 
+/* Device allocations (cudaMalloc calls, successful or not) the library has made in
+ * this process, all handles together: every device buffer of the library goes through
+ * one allocator that counts them.  No counterpart in the reference; a diagnostic for
+ * callers that must know that a call allocates nothing. */
+uint64_t mpcd_gb_device_allocations(void);
+
 /* ---- allocation-free cell offsets (no counterpart in the reference) ---- */
 
 /* Largest cell count (C) that mpcd_gb_cell_offsets_noalloc accepts. */

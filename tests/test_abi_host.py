@@ -97,5 +97,5 @@ def test_null_handle_is_rejected_everywhere():
     declared = set(capi.declared_symbols())
     covered = set(calls) | {"mpcd_gb_num_particles", "mpcd_gb_num_cells", "mpcd_gb_num_boxes",
                             "mpcd_gb_step_index", "mpcd_gb_destroy", "mpcd_gb_abi_version", "mpcd_gb_create",
-                            "mpcd_gb_ensemble_create", "mpcd_gb_last_error"}
+                            "mpcd_gb_ensemble_create", "mpcd_gb_last_error", "mpcd_gb_device_allocations"}
     assert declared == covered, declared ^ covered

@@ -4,7 +4,9 @@ The entry point writes, into a caller's device buffer, where each cell's run
 starts in the mpcd_gb_dump_layout order; its scan scratch is a fixed array in
 the library's device memory.  Every case calls it twice in a row and compares
 both results with the offsets implied by mpcd_gb_dump_layout, so a scratch that
-is not re-zeroed between calls shows up as a mismatch of the second call.
+is not re-zeroed between calls shows up as a mismatch of the second call.  The
+library's count of its device allocations (mpcd_gb_device_allocations: every device
+buffer goes through one counting allocator) must not move across a call.
 """
 from __future__ import annotations
 
@@ -60,18 +62,19 @@ CASES = [
 
 @pytest.mark.parametrize("L,periodic,n,alg", CASES)
 def test_offsets_match_dump_on_consecutive_calls(L, periodic, n, alg):
-    torch = pytest.importorskip("torch")
+    before_handle = capi.device_allocations()
     h = capi.Handle(L=L, periodic=periodic, n=n, algorithm=alg, drag=0.001 * (periodic[2] == 0), seed=11)
+    assert capi.device_allocations() > before_handle   # the counter sees the handle's buffers
     try:
         first, second = _device_buffer(h.C + 1), _device_buffer(h.C + 1)
         for _ in range(2):
             h.step(3)
             h.cell_offsets_noalloc(first.data_ptr(), h.C + 1)
             h.synchronize()
-            free_before = torch.cuda.mem_get_info()[0]
+            allocations = capi.device_allocations()
             h.cell_offsets_noalloc(second.data_ptr(), h.C + 1)
             h.synchronize()
-            assert torch.cuda.mem_get_info()[0] == free_before
+            assert capi.device_allocations() == allocations   # every device buffer is counted
             expected = _offsets_from_dump(h, L, n)
             assert np.array_equal(_read(h, first), expected)
             assert np.array_equal(_read(h, second), expected)
