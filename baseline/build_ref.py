@@ -12,11 +12,12 @@ Steps
                  checkout -- ``MPCD_REFERENCE_ROOT``, else a checkout named
                  ``reference`` beside this repository -- into
                  ``baseline/_ref/tree``, and a second copy into
-                 ``baseline/_ref/tree_dropin`` with the two changes that
-                 INTEGRATION.md documents (section 1: the GbBackend class,
-                 written to src/libmpcd/gb300_backend/gb300_backend.hpp;
-                 section 2: its diff applied to backend_factory.hpp), both
-                 read from INTEGRATION.md itself.  Machines without the
+                 ``baseline/_ref/tree_dropin`` with the two changes a maintainer
+                 makes to the reference: the GbBackend class
+                 (``baseline/dropin/gb300_backend.hpp``, written to
+                 src/libmpcd/gb300_backend/gb300_backend.hpp) and the factory
+                 diff (``baseline/dropin/backend_factory.diff``, applied to
+                 src/libmpcd/common/backend_factory.hpp).  Machines without the
                  checkout build from the staged copies.
   build_stock()  ``baseline/_ref/stock/pympcd``: the reference's binding,
                  SimulationHandle, CPU backend and CUDA backend, unchanged, as
@@ -86,17 +87,17 @@ def module_path(kind: str) -> str:
 
 # ---------------------------------------------------------------- staging
 
-def _integration_blocks() -> tuple[str, str]:
-    """The GbBackend class (section 1) and the factory diff (section 2) of INTEGRATION.md."""
-    with open(os.path.join(ROOT, "INTEGRATION.md")) as f:
-        text = f.read()
-    sec1 = text[text.index("## 1."):text.index("## 2.")]
-    sec2 = text[text.index("## 2."):text.index("## 3.")]
-    cls = re.search(r"```cpp\n(.*?)```", sec1, re.S)
-    diff = re.search(r"```diff\n(.*?)```", sec2, re.S)
-    if not cls or not diff:
-        raise RuntimeError("INTEGRATION.md: the section 1 class or the section 2 diff is missing")
-    return cls.group(1), diff.group(1)
+DROPIN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "dropin")
+
+
+def dropin_sources() -> tuple[str, str]:
+    """The GbBackend class and the factory diff that turn the reference into a
+    client of libmpcd_gb.so (baseline/dropin/)."""
+    with open(os.path.join(DROPIN, "gb300_backend.hpp")) as f:
+        cls = f.read()
+    with open(os.path.join(DROPIN, "backend_factory.diff")) as f:
+        diff = f.read()
+    return cls, diff
 
 
 def apply_unified_diff(original: str, diff: str) -> str:
@@ -136,7 +137,7 @@ def stage(force: bool = False) -> bool:
     root = reference_root()
     if not _checkout_present(root):
         return False
-    cls, diff = _integration_blocks()
+    cls, diff = dropin_sources()
     for tree in (TREE, TREE_DROPIN):
         if force and os.path.isdir(tree):
             shutil.rmtree(tree)
@@ -144,7 +145,7 @@ def stage(force: bool = False) -> bool:
             src, dst = os.path.join(root, rel), os.path.join(tree, rel)
             if os.path.isdir(src):
                 shutil.copytree(src, dst, dirs_exist_ok=True)
-    # the drop-in tree: INTEGRATION.md sections 1 and 2, nothing else
+    # the drop-in tree: the GbBackend class and the factory diff, nothing else
     lib = os.path.join(TREE_DROPIN, "src", "libmpcd")
     os.makedirs(os.path.join(lib, "gb300_backend"), exist_ok=True)
     _write_if_changed(os.path.join(lib, "gb300_backend", "gb300_backend.hpp"), cls)
@@ -257,7 +258,7 @@ def build_stock() -> str:
 
 
 def build_dropin() -> str:
-    """The reference's binding and SimulationHandle over libmpcd_gb.so."""
+    """The reference's binding and SimulationHandle over libmpcd_gb.so (baseline/dropin/)."""
     if not staged():
         raise RuntimeError("reference sources are not staged (baseline/_ref/tree_dropin)")
     gb_lib = os.path.join(ROOT, "cudampcd_gb300", "libmpcd_gb.so")

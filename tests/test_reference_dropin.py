@@ -2,8 +2,9 @@
 
 baseline/build_ref.py compiles the reference's unchanged src/bindings/bindings.cpp,
 SimulationHandle (src/libmpcd/api/simulator_handle.cpp) and CPU backend, with the
-GbBackend class and the factory diff that INTEGRATION.md documents, against
-libmpcd_gb.so (baseline/_ref/dropin/pympcd).  These tests import that module in a
+GbBackend class (baseline/dropin/gb300_backend.hpp) and the factory diff
+(baseline/dropin/backend_factory.diff), against libmpcd_gb.so
+(baseline/_ref/dropin/pympcd).  These tests import that module in a
 child process (the reference's module is also named `pympcd`, and pybind11 keeps
 one registration of its classes per process) and run the flows of the reference's
 own integration tests (tests/python/test_integration.py: a basic run, positions
