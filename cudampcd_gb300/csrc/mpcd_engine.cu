@@ -113,6 +113,13 @@ public:
         check(cudaSetDevice((int)params_.device_id), "cudaSetDevice");
         check(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking), "cudaStreamCreate");
         stream_ = own_stream_;
+        if (box_params_.size() > 1) {   // ensembles: the batch classes' side streams
+            for (int i = 0; i < 2; ++i) {
+                check(cudaStreamCreateWithFlags(&branches_.side[i], cudaStreamNonBlocking), "cudaStreamCreate");
+                check(cudaEventCreateWithFlags(&branches_.join[i], cudaEventDisableTiming), "cudaEventCreate");
+            }
+            check(cudaEventCreateWithFlags(&branches_.fork, cudaEventDisableTiming), "cudaEventCreate");
+        }
         cudaDeviceProp prop;
         check(cudaGetDeviceProperties(&prop, (int)params_.device_id), "cudaGetDeviceProperties");
         sms_ = prop.multiProcessorCount;
@@ -128,6 +135,14 @@ public:
             cudaStreamSynchronize(own_stream_);
             cudaStreamDestroy(own_stream_);
         }
+        for (int i = 0; i < 2; ++i) {
+            if (branches_.side[i]) {
+                cudaStreamSynchronize(branches_.side[i]);
+                cudaStreamDestroy(branches_.side[i]);
+            }
+            if (branches_.join[i]) cudaEventDestroy(branches_.join[i]);
+        }
+        if (branches_.fork) cudaEventDestroy(branches_.fork);
     }
 
     // ------------------------------------------------------------ reference Backend interface
@@ -1118,7 +1133,7 @@ private:
             a.sample = sample ? 1 : 0;
             use_run_kernel_ghosts(a, false);
             err = select_overflow(a, (uint64_t)i, cs);
-            if (err == cudaSuccess) err = launch_step(a, params_.algorithm, false, pbuf_, grid_, cs);
+            if (err == cudaSuccess) err = launch_step(a, params_.algorithm, false, pbuf_, grid_, cs, &branches_);
             if (err == cudaSuccess && sample)
                 err = launch_sample_finalize(samp_.as<float4>(), acc_.as<SampleAcc>(), cells_, 0, sms_ * 8, cs);
         }
@@ -1176,7 +1191,7 @@ private:
         use_run_kernel_ghosts(a, use_table_);
         check(select_overflow(a, step_, stream_), "overflow selection");
         if (before) check(cudaEventRecord(before, stream_), "event");
-        check(launch_step(a, params_.algorithm, use_table_, pbuf_, grid_, stream_), "step kernel");
+        check(launch_step(a, params_.algorithm, use_table_, pbuf_, grid_, stream_, &branches_), "step kernel");
         if (after) check(cudaEventRecord(after, stream_), "event");
         last_step_table_ = use_table_;   // a replay of this step must consume the same draws
         use_table_ = false;
@@ -1332,6 +1347,7 @@ private:
     mpcd_gb_params params_;                 // box 0 (algorithm and device of every box)
     std::vector<mpcd_gb_params> box_params_;
     cudaStream_t own_stream_ = nullptr, stream_ = nullptr;
+    RunBranches branches_;   // ensembles: side streams of the batch classes
     int sms_ = 0, grid_ = 0;
     std::vector<BoxDesc> boxes_;
     uint64_t N_ = 0, cells_ = 0, tiles_ = 0, total_slots_ = 0, walls_ = 0;

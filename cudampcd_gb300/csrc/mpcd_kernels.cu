@@ -1981,22 +1981,38 @@ bool run_kernel_takes(const StepArgs& a, int algorithm, bool table)
            (a.nboxes == 1 || (a.run_info && a.box_shifts)) && a.boxes_n_max <= kRunMaxN;
 }
 
-cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st)
+cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st,
+                        const RunBranches* branches)
 {
     if (a.run_kernel) {
         // one launch per batch size in use: a single box's, or an ensemble's density
-        // classes, whose runs the run table lists class by class
-        bool first = true;
-        for (int cls = 0; cls < 3; ++cls) {
-            const uint32_t r0 = a.run_class[cls], r1 = a.run_class[cls + 1];
-            if (r0 >= r1) continue;
-            const StepFnRun f = kRunFns[a.sample ? 1 : 0][a.nboxes == 1 ? 1 : 0][cls];
-            f<<<grid, kThreads, 0, st>>>(a, r0, r1, first);
-            first = false;
-            const cudaError_t e = cudaGetLastError();
+        // classes, whose runs the run table lists class by class; with branches, the
+        // second and third class on side streams (the classes share no cell and no
+        // count: every write is an atomic claim or a lane's own cell)
+        int used[3], nused = 0;
+        for (int cls = 0; cls < 3; ++cls)
+            if (a.run_class[cls] < a.run_class[cls + 1]) used[nused++] = cls;
+        const bool fork = branches && branches->side[0] && branches->side[1] && nused > 1;
+        cudaError_t e = cudaSuccess;
+        if (fork) {
+            e = cudaEventRecord(branches->fork, st);
+            for (int i = 1; i < nused && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(branches->side[i - 1], branches->fork, 0);
             if (e != cudaSuccess) return e;
         }
-        return cudaSuccess;
+        for (int i = 0; i < nused; ++i) {
+            const int cls = used[i];
+            const StepFnRun f = kRunFns[a.sample ? 1 : 0][a.nboxes == 1 ? 1 : 0][cls];
+            f<<<grid, kThreads, 0, fork && i > 0 ? branches->side[i - 1] : st>>>(a, a.run_class[cls],
+                                                                                    a.run_class[cls + 1], i == 0);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
+        if (fork) {
+            for (int i = 1; i < nused && e == cudaSuccess; ++i) {
+                e = cudaEventRecord(branches->join[i - 1], branches->side[i - 1]);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(st, branches->join[i - 1], 0);
+            }
+        }
+        return e;
     }
     const size_t smem = step_smem_bytes(pbuf, a.boxes_tile_cells, algorithm);
     kStepFns[algorithm ? 1 : 0][table ? 1 : 0][a.nboxes == 1 ? 1 : 0][a.replay ? 1 : 0]<<<grid, kThreads, smem, st>>>(

@@ -14,8 +14,17 @@ namespace mpcd_gb {
 size_t step_smem_bytes(uint32_t pbuf, uint32_t cells, int algorithm);
 // Opt the step kernels into that much shared memory and report resident CTAs per SM.
 cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* blocks_per_sm);
+// Side streams on which an ensemble's second and third batch classes run beside the
+// first: the step's stream forks to them and joins them again, so that each class's
+// launch fills the tail of the one before it.  Null streams: one after another.
+struct RunBranches {
+    cudaStream_t side[2] = {nullptr, nullptr};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[2] = {nullptr, nullptr};
+};
 // One step of every box (algorithm 0 = SRD, 1 = extended; table = injected draws).
-cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st);
+cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st,
+                        const RunBranches* branches = nullptr);
 // Whether srd_run_kernel can run this step (SRD, Philox draws, no replay, tape
 // or pressure estimator, n <= 64 in every box, a run table for ensembles and the
 // wall-ghost array when boxes have walls); the caller then sets a.run_kernel,
