@@ -30,11 +30,12 @@ L^2 n g / (8 max u)) and with the curvature fit.
 
 Profiling options (the default run uses none of them): --size LX LY LZ replaces
 the fluid cells of the workload (walls are added in z), --algorithm extended
-switches the collision, --no-e2e and --no-cpu skip those parts.
+switches the collision, --no-e2e, --no-cpu and --no-adjoint skip those parts.
 
 Adjoint: --adjoint times the differentiable channel (64 x 64 x 32 cells + 2 walls,
 n = 10, 200 steps, checkpoints every 20): a plain step, the sampled forward with
-checkpoints, and the adjoint (backward) per step, and their ratios.
+checkpoints, and the adjoint (backward) per step, and their ratios.  The default
+line carries the same figures in its `adjoint` block.
 
 One JSON line on rank 0.  `value` is device-timed particle-steps/s with the
 state resident in HBM; `e2e` is the same metric through the Python API the
@@ -599,6 +600,8 @@ def run_gpu_arm(args, rank, world, local_rank):
             out["reference_gpu"] = ref_gpu
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline_block(1, args.steps_cpu)
+        if world == 1 and not args.no_adjoint:
+            out["adjoint"] = adjoint_block(5)   # the adjoint's cost against a plain step (config 5)
         print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -834,7 +837,10 @@ def run_viscosity(args):
     print(json.dumps(out), flush=True)
 
 
-def run_adjoint(args):
+ADJOINT_WORKLOAD = dict(L=(64, 64, 34), n=10, drag=1e-3, dt=0.02, seed=5, steps=200, every=20)
+
+
+def adjoint_block(warmup: int) -> dict:
     """The differentiable channel (64 x 64 x 32 cells + 2 walls, n = 10, dt = 0.02,
     200 sampled steps, checkpoints every 20): CUDA-event times of a plain step,
     of the sampled forward with checkpoints, and of the adjoint; the adjoint's
@@ -846,7 +852,8 @@ def run_adjoint(args):
     from cudampcd_gb300 import capi
     from cudampcd_gb300.adjoint import channel_profile
 
-    L, n, drag0, dt, seed, S, K = (64, 64, 34), 10, 1e-3, 0.02, 5, 200, 20
+    w = ADJOINT_WORKLOAD
+    L, n, drag0, dt, seed, S, K = w["L"], w["n"], w["drag"], w["dt"], w["seed"], w["steps"], w["every"]
     h = capi.Handle(L=L, periodic=(1, 1, 0), n=n, dt=dt, drag=drag0, seed=seed)
     N = h.N
     pos = torch.from_numpy(h.positions()).cuda()
@@ -856,7 +863,7 @@ def run_adjoint(args):
     z = torch.arange(L[2], dtype=torch.float64, device="cuda") + 0.5 - L[2] / 2.0
     target = 1.1 * n * drag0 * (hz * hz - z * z) / (2.0 * eta)
     # plain steps (two launches each), timed on the handle's stream
-    h.step(max(args.warmup, 6))
+    h.step(max(warmup, 6))
     total_ms, _ = h.time_steps(S)
     plain = total_ms / S
     fw, bw = [], []
@@ -878,18 +885,25 @@ def run_adjoint(args):
         assert torch.isfinite(v0.grad).all()
     h.close()
     fwd, bwd = statistics.median(fw), statistics.median(bw)
-    out = {"metric": METRIC, "value": N / (bwd * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": S,
-           "warmup": args.warmup, "ms_per_step": bwd, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": f"differentiable SRD channel {L[0]}x{L[1]}x{L[2] - 2} cells + 2 walls, n={n}, "
-                                  f"N={N}, dt={dt}, g={drag0}, {S} sampled steps, checkpoints every {K}; loss = MSE "
-                                  f"of U(z) against 1.1 x the analytic parabola; gradients w.r.t. g and all V0",
-                      "timing": "plain steps: CUDA events on the handle's stream; forward and backward: host wall "
-                                "clock around each call (both synchronise), median of 3 after one untimed pass"},
-           "adjoint": {"plain_ms_per_step": plain, "forward_ms_per_step": fwd, "backward_ms_per_step": bwd,
-                       "backward_over_plain": bwd / plain, "backward_over_forward": bwd / fwd,
-                       "forward_plus_backward_over_plain": (fwd + bwd) / plain,
-                       "value_meaning": "value = particle-steps/s of the adjoint (backward) sweep"}}
+    return {"workload": f"differentiable SRD channel {L[0]}x{L[1]}x{L[2] - 2} cells + 2 walls, n={n}, N={N}, "
+                        f"dt={dt}, g={drag0}, {S} sampled steps, checkpoints every {K}; loss = MSE of U(z) against "
+                        f"1.1 x the analytic parabola; gradients w.r.t. g and all V0",
+            "timing": "plain steps: CUDA events on the handle's stream; forward and backward: host wall clock "
+                      "around each call (both synchronise), median of 3 after one untimed pass",
+            "particles": N, "plain_ms_per_step": plain, "forward_ms_per_step": fwd, "backward_ms_per_step": bwd,
+            "backward_over_plain": bwd / plain, "backward_over_forward": bwd / fwd,
+            "forward_plus_backward_over_plain": (fwd + bwd) / plain}
+
+
+def run_adjoint(args):
+    """The adjoint line: value = particle-steps/s of the adjoint (backward) sweep."""
+    a = adjoint_block(args.warmup)
+    bwd = a["backward_ms_per_step"]
+    out = {"metric": METRIC, "value": a["particles"] / (bwd * 1e-3), "unit": UNIT, "n_gpus": 1,
+           "steps": ADJOINT_WORKLOAD["steps"], "warmup": args.warmup, "ms_per_step": bwd, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": a["workload"], "timing": a["timing"]},
+           "adjoint": {k: v for k, v in a.items() if k not in ("workload", "timing")}}
     print(json.dumps(out), flush=True)
 
 
@@ -905,6 +919,7 @@ def main():
     ap.add_argument("--steps-cpu", dest="steps_cpu", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", dest="no_adjoint", action="store_true")
     ap.add_argument("--size", type=int, nargs=3, metavar=("LX", "LY", "LZ"))
     ap.add_argument("--algorithm", default="srd", choices=["srd", "extended"])
     ap.add_argument("--ensemble", type=int, default=0, metavar="R")
