@@ -1247,6 +1247,7 @@ private:
             a.tape_key = tkey_.as<uint32_t>() + (size_t)i * N_;
             a.tape_lab = tlab_.as<uint32_t>() + (size_t)i * N_;
             a.tape_ncell = tncell_.as<uint32_t>() + (size_t)i * cells_;
+            use_run_kernel_ghosts(a, false);   // the run kernel records the tape of single-box SRD steps
             check(select_overflow(a, step_, stream_), "overflow selection");
             check(launch_step(a, params_.algorithm, false, pbuf_, grid_, stream_), "tape step");
             check(launch_sample_finalize(samp_.as<float4>(), acc_.as<SampleAcc>(), cells_, 1, sms_ * 8, stream_,

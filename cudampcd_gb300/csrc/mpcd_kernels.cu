@@ -1161,8 +1161,9 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(const StepArgs a, uin
 
 // ------------------------------------------------------------------ SRD run kernel
 //
-// The production SRD step of one box (Philox draws; replays, the adjoint tape
-// and the pressure estimator take step_kernel): one warp per run of 32
+// The production SRD step of one box or an ensemble (Philox draws; replays and the
+// pressure estimator take step_kernel; TAPE: a sampled single-box step that records
+// the adjoint tape, as step_kernel does): one warp per run of 32
 // consecutive cells (storage order), lane l owning cell l of the run.  No
 // CTA-wide barrier and no staging: each warp works alone on its runs with 1.5
 // KB of shared memory of its own, and reads the particles straight from their
@@ -1215,7 +1216,7 @@ __device__ __forceinline__ uint2 run_entry(const StepArgs& a, uint32_t run)
     return make_uint2(a.box0.cell_base + c0, min(kRunCells, a.box0.C - c0));
 }
 
-template <bool SAMPLE, bool SINGLE, uint32_t BATCH>
+template <bool SAMPLE, bool SINGLE, uint32_t BATCH, bool TAPE = false>
 __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, uint32_t run_begin, uint32_t run_end,
                                                               bool first_launch)
 {
@@ -1294,6 +1295,7 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
             sh.gsum[lane][2] = gz;
         }
         const uint32_t m = cnt + ng;   // entries of the cell's collision
+        if (TAPE && valid) a.tape_ncell[cur.x + lane] = m > 1 ? m : 0u;   // the adjoint tape: entries of collided cells
         if (m > 1) {
             const float3 ax = srd_axis_philox(b, step, ref_index(b, cc));
             sh.axis[lane] = make_float4(ax.x, ax.y, ax.z, 0.0f);
@@ -1411,7 +1413,13 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
                 xn = stream_shift(b, x, vn, sn);
                 key = b.cell_base + storage_index(b, cell_of_wrapped(b, xn));
                 id = __float_as_uint(vp.w);
-                if (SAMPLE) sample_add(a.samp, b.cell_base + storage_index(b, cell_of_wrapped(b, x)), v, true);
+                const uint32_t lab = SAMPLE || TAPE ? b.cell_base + storage_index(b, cell_of_wrapped(b, x)) : 0u;
+                if (SAMPLE) sample_add(a.samp, lab, v, true);
+                if (TAPE) {   // collision cell (or none), lab cell and the bounce of the streaming that follows
+                    const bool bounced = vn.x != v.x || vn.y != v.y || vn.z != v.z;
+                    a.tape_key[id] = __float_as_uint(cd.w) > 1 ? cur.x + i : kTapeNone;
+                    a.tape_lab[id] = lab | (bounced ? kTapeBounce : 0u);
+                }
             }
             store_particle(a, b, xn, vn, id, key, active);
         }
@@ -1969,6 +1977,9 @@ const StepFn kStepFns[2][2][2][2] = {
 
 using StepFnRun = void (*)(const StepArgs, uint32_t, uint32_t, bool);
 // [sample][single box][batch class: 16, 8, 4 cells]
+// single-box sampled steps that record the adjoint tape, by batch size
+static const StepFnRun kRunTapeFns[3] = {srd_run_kernel<true, true, 16, true>, srd_run_kernel<true, true, 8, true>,
+                                         srd_run_kernel<true, true, 4, true>};
 static const StepFnRun kRunFns[2][2][3] = {
     {{srd_run_kernel<false, false, 16>, srd_run_kernel<false, false, 8>, srd_run_kernel<false, false, 4>},
      {srd_run_kernel<false, true, 16>, srd_run_kernel<false, true, 8>, srd_run_kernel<false, true, 4>}},
@@ -1977,8 +1988,9 @@ static const StepFnRun kRunFns[2][2][3] = {
 
 bool run_kernel_takes(const StepArgs& a, int algorithm, bool table)
 {
-    return algorithm == 0 && !table && !a.replay && !a.tape_key && !a.pressure && (a.ghosts || !a.total_walls) &&
-           (a.nboxes == 1 || (a.run_info && a.box_shifts)) && a.boxes_n_max <= kRunMaxN;
+    return algorithm == 0 && !table && !a.replay && (!a.tape_key || (a.nboxes == 1 && a.sample)) && !a.pressure &&
+           (a.ghosts || !a.total_walls) && (a.nboxes == 1 || (a.run_info && a.box_shifts)) &&
+           a.boxes_n_max <= kRunMaxN;
 }
 
 cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st,
@@ -2001,7 +2013,7 @@ cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t p
         }
         for (int i = 0; i < nused; ++i) {
             const int cls = used[i];
-            const StepFnRun f = kRunFns[a.sample ? 1 : 0][a.nboxes == 1 ? 1 : 0][cls];
+            const StepFnRun f = a.tape_key ? kRunTapeFns[cls] : kRunFns[a.sample ? 1 : 0][a.nboxes == 1 ? 1 : 0][cls];
             f<<<grid, kThreads, 0, fork && i > 0 ? branches->side[i - 1] : st>>>(a, a.run_class[cls],
                                                                                     a.run_class[cls + 1], i == 0);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -2060,6 +2072,8 @@ cudaError_t configure_step(int algorithm, uint32_t pbuf, uint32_t cells, int* bl
                 if (e == cudaSuccess)
                     e = cudaFuncSetAttribute((const void*)kRunFns[i][j][k], cudaFuncAttributePreferredSharedMemoryCarveout,
                                              27);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+        e = cudaFuncSetAttribute((const void*)kRunTapeFns[k], cudaFuncAttributePreferredSharedMemoryCarveout, 27);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, (const void*)sample_finalize_kernel);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, (const void*)overflow_select_kernel);
     if (e != cudaSuccess) return e;

@@ -25,10 +25,10 @@ struct RunBranches {
 // One step of every box (algorithm 0 = SRD, 1 = extended; table = injected draws).
 cudaError_t launch_step(const StepArgs& a, int algorithm, bool table, uint32_t pbuf, int grid, cudaStream_t st,
                         const RunBranches* branches = nullptr);
-// Whether srd_run_kernel can run this step (SRD, Philox draws, no replay, tape
-// or pressure estimator, n <= 64 in every box, a run table for ensembles and the
-// wall-ghost array when boxes have walls); the caller then sets a.run_kernel,
-// which launch_step and the step's prologue follow.
+// Whether srd_run_kernel can run this step (SRD, Philox draws, no replay or
+// pressure estimator, the adjoint tape only for one sampled box, n <= 64 in every
+// box, a run table for ensembles and the wall-ghost array when boxes have walls);
+// the caller then sets a.run_kernel, which launch_step and the step's prologue follow.
 bool run_kernel_takes(const StepArgs& a, int algorithm, bool table);
 // state->step_base += steps (the last node of a replayed step graph).
 cudaError_t launch_advance(DeviceState* state, unsigned steps, cudaStream_t st);
