@@ -1226,7 +1226,7 @@ private:
         need(tcnt_, sizeof(uint32_t) * cells_ * K, "alloc tape");
         need(tb0_, sizeof(uint32_t) * N_, "alloc tape");
         need(lam_, sizeof(float) * 3 * N_, "alloc adjoint");
-        need(cellsum_, sizeof(float4) * cells_, "alloc adjoint");
+        need(cellsum_, sizeof(float4) * cells_ * 2, "alloc adjoint");   // cell sums, then axes and sampling terms
         need(gsum_, sizeof(double), "alloc adjoint");
     }
 

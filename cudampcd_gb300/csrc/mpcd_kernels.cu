@@ -1888,22 +1888,38 @@ __global__ void __launch_bounds__(kThreads) profile_kernel(const SampleAcc* acc,
     if (threadIdx.x == 0) profile[blockIdx.x] = (float)(red[0] * inv);
 }
 
+// Per cell of the step (storage order): clear the cell sums of mu, and store the
+// cell's rotation axis (as a collision cell) and its sampling term dU(z) w / count
+// (as a lab cell; FP64 quotient rounded to FP32) in cell_axis, so that the particle
+// passes read them instead of drawing an axis and dividing per particle.
+__global__ void __launch_bounds__(kThreads) adjoint_cells_kernel(BoxDesc b, uint64_t step, const uint32_t* lab_count,
+                                                                 const float* dU, double w, float4* cellsum,
+                                                                 float4* cell_axis)
+{
+    const uint32_t Lz = (uint32_t)b.L[2];
+    for (uint32_t c = blockIdx.x * kThreads + threadIdx.x; c < b.C; c += gridDim.x * kThreads) {
+        cellsum[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const uint32_t cnt = lab_count[b.cell_base + c];
+        const float term = cnt ? (float)((double)dU[c % Lz] * w / (double)cnt) : 0.0f;   // z fastest
+        const float3 a = srd_axis_philox(b, step, ref_index(b, storage_coords(b, c)));
+        cell_axis[c] = make_float4(a.x, a.y, a.z, term);
+    }
+}
+
 // mu = B_{t+1} lambda + sampling term; cell sums of mu over collided particles; dL/dg partial.
 __global__ void __launch_bounds__(kThreads) adjoint_pass1_kernel(BoxDesc b, uint32_t n, float* lam,
                                                                  const uint32_t* key, const uint32_t* lab,
-                                                                 const uint32_t* lab_count, const float* dU,
-                                                                 double w, float4* cellsum, double* gsum)
+                                                                 const float4* cell_axis, float4* cellsum,
+                                                                 double* gsum)
 {
     __shared__ double red[kThreads];
     double gl = 0;
-    const uint32_t Lz = (uint32_t)b.L[2];
     for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
         float3 m = make_float3(lam[3 * i], lam[3 * i + 1], lam[3 * i + 2]);
         const uint32_t l = lab[i];
         if (l & kTapeBounce) m = make_float3(-m.x, -m.y, -m.z);
         const uint32_t c = l & ~kTapeBounce;
-        const uint32_t z = (c - b.cell_base) % Lz;   // lab cells in storage order (z fastest)
-        m.x += (float)((double)dU[z] * w / (double)lab_count[c]);
+        m.x += __ldg(&cell_axis[c - b.cell_base].w);
         lam[3 * i] = m.x; lam[3 * i + 1] = m.y; lam[3 * i + 2] = m.z;
         const uint32_t k = key[i];
         if (k != kTapeNone) {
@@ -1921,9 +1937,9 @@ __global__ void __launch_bounds__(kThreads) adjoint_pass1_kernel(BoxDesc b, uint
 }
 
 // lambda = R^T (mu - s_c) + s_c for collided particles (R^T: rotation by -alpha).
-__global__ void __launch_bounds__(kThreads) adjoint_pass2_kernel(BoxDesc b, uint64_t step, uint32_t n, float* lam,
+__global__ void __launch_bounds__(kThreads) adjoint_pass2_kernel(BoxDesc b, uint32_t n, float* lam,
                                                                  const uint32_t* key, const uint32_t* ncell,
-                                                                 const float4* cellsum)
+                                                                 const float4* cellsum, const float4* cell_axis)
 {
     for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
         const uint32_t k = key[i];
@@ -1931,7 +1947,8 @@ __global__ void __launch_bounds__(kThreads) adjoint_pass2_kernel(BoxDesc b, uint
         const float inv = 1.0f / (float)ncell[k];
         const float4 cs = cellsum[k];
         const float3 sc = make_float3(cs.x * inv, cs.y * inv, cs.z * inv);
-        const float3 a = srd_axis_philox(b, step, ref_index(b, storage_coords(b, k - b.cell_base)));
+        const float4 ax = __ldg(&cell_axis[k - b.cell_base]);
+        const float3 a = make_float3(ax.x, ax.y, ax.z);
         const float3 wv = make_float3(lam[3 * i] - sc.x, lam[3 * i + 1] - sc.y, lam[3 * i + 2] - sc.z);
         const float d = dot3(wv, a);
         const float3 para = make_float3(a.x * d, a.y * d, a.z * d);
@@ -2092,11 +2109,11 @@ cudaError_t launch_adjoint_step(const BoxDesc& b, uint64_t step, uint64_t sample
                                 const uint32_t* lab, const uint32_t* ncell, const uint32_t* lab_count,
                                 const float* dU, float4* cellsum, double* gsum, int grid, cudaStream_t st)
 {
-    cudaError_t e = cudaMemsetAsync(cellsum, 0, sizeof(float4) * b.C, st);
-    if (e != cudaSuccess) return e;
     const double w = 1.0 / ((double)samples * (double)b.L[0] * (double)b.L[1]);
-    adjoint_pass1_kernel<<<grid, kThreads, 0, st>>>(b, b.N, lam, key, lab, lab_count, dU, w, cellsum, gsum);
-    adjoint_pass2_kernel<<<grid, kThreads, 0, st>>>(b, step, b.N, lam, key, ncell, cellsum);
+    float4* const cell_axis = cellsum + b.C;
+    adjoint_cells_kernel<<<grid, kThreads, 0, st>>>(b, step, lab_count, dU, w, cellsum, cell_axis);
+    adjoint_pass1_kernel<<<grid, kThreads, 0, st>>>(b, b.N, lam, key, lab, cell_axis, cellsum, gsum);
+    adjoint_pass2_kernel<<<grid, kThreads, 0, st>>>(b, b.N, lam, key, ncell, cellsum, cell_axis);
     return cudaGetLastError();
 }
 

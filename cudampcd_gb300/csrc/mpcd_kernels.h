@@ -52,6 +52,7 @@ cudaError_t launch_mean_fields(const SampleAcc* acc, const BoxDesc& b, double in
 // sums of `samples` steps; one reverse step (both passes) at absolute step `step`;
 // dL/dV0 from the final adjoint and the bounce bits of the initial streaming.
 cudaError_t launch_profile(const SampleAcc* acc, const BoxDesc& b, uint64_t samples, float* profile, cudaStream_t st);
+// cellsum: 2 C entries (the cell sums of mu, then each cell's axis and sampling term).
 cudaError_t launch_adjoint_step(const BoxDesc& b, uint64_t step, uint64_t samples, float* lam, const uint32_t* key,
                                 const uint32_t* lab, const uint32_t* ncell, const uint32_t* lab_count,
                                 const float* dU, float4* cellsum, double* gsum, int grid, cudaStream_t st);
