@@ -99,6 +99,33 @@ def test_shallow_buckets_change_nothing(name):
         b.close()
 
 
+# boxes large enough that every warp of the run kernel and every CTA of the tile
+# kernel sweeps many runs or tiles, with about one cell in six (n = 20, depth 24)
+# spilled into the extension area each step
+LARGE = {
+    "srd_160x160x20": (dict(L=(160, 160, 22), periodic=(1, 1, 0), n=20, drag=1e-3, seed=31), 24),
+    "ext_100x100x20": (dict(L=(100, 100, 22), periodic=(1, 1, 0), n=20, algorithm=1, drag=5e-4, seed=32), 24),
+}
+
+
+@pytest.mark.parametrize("name", list(LARGE))
+def test_shallow_buckets_in_large_boxes(name):
+    kw, depth = LARGE[name]
+    a, b = _pair(depth, **kw)
+    try:
+        a.step(1)
+        b.step(1)
+        _same_state(a, b, "after one step")
+        a.step(6)   # one graph replay
+        b.step(6)
+        _same_state(a, b, "after a graph replay")
+        assert a.counters()[1] == 0 and b.counters()[1] == 0
+        assert b.counters()[0] > 10 * max(a.counters()[0], 1000)
+    finally:
+        a.close()
+        b.close()
+
+
 def test_shallow_buckets_with_every_particle_in_one_cell():
     """All particles of a 10^3, n = 10 box in one cell: that cell's 40 lowest ids
     collide, the others skip the collision (the reference's index-order table)."""
