@@ -139,8 +139,14 @@ __device__ __forceinline__ uint32_t cell_coord_wrapped(float x, float Lh, uint32
     return c == L ? 0u : (uint32_t)(long long)f % L;
 }
 
+// One branch for the three axes on the common path (each axis's own slow path
+// recomputes the same floor, so the result is cell_coord_wrapped's on every axis).
 __device__ __forceinline__ uint3 cell_of_wrapped(const BoxDesc& b, float3 x)
 {
+    const float fx = floorf(x.x + b.Lh[0]), fy = floorf(x.y + b.Lh[1]), fz = floorf(x.z + b.Lh[2]);
+    const uint32_t cx = (uint32_t)(int)fx, cy = (uint32_t)(int)fy, cz = (uint32_t)(int)fz;
+    if (__builtin_expect((cx < (uint32_t)b.L[0]) & (cy < (uint32_t)b.L[1]) & (cz < (uint32_t)b.L[2]), 1))
+        return make_uint3(cx, cy, cz);
     return make_uint3(cell_coord_wrapped(x.x, b.Lh[0], (uint32_t)b.L[0]),
                       cell_coord_wrapped(x.y, b.Lh[1], (uint32_t)b.L[1]),
                       cell_coord_wrapped(x.z, b.Lh[2], (uint32_t)b.L[2]));

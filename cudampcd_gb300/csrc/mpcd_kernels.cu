@@ -160,17 +160,13 @@ __device__ __forceinline__ int box_of_particle(const BoxDesc* boxes, int nboxes,
 // are served by one atomic (warp-aggregated).  Returns the slot.
 __device__ __forceinline__ uint32_t claim_slot(uint32_t* count, uint32_t key, bool active)
 {
-    const unsigned act = __ballot_sync(kFull, active);
-    uint32_t slot = 0;
-    if (active) {
-        const unsigned peers = __match_any_sync(act, key);
-        const int leader = __ffs(peers) - 1;
-        uint32_t base = 0;
-        if ((int)(threadIdx.x & 31) == leader) base = atomicAdd(count + key, (uint32_t)__popc(peers));
-        base = __shfl_sync(peers, base, leader);
-        slot = base + (uint32_t)__popc(peers & lanemask_lt());
-    }
-    return slot;
+    // idle lanes share a key no cell has, so that the whole warp takes one path
+    const unsigned peers = __match_any_sync(kFull, active ? key : 0xFFFFFFFFu);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (active && (int)(threadIdx.x & 31) == leader) base = atomicAdd(count + key, (uint32_t)__popc(peers));
+    base = __shfl_sync(kFull, base, leader);
+    return base + (uint32_t)__popc(peers & lanemask_lt());
 }
 
 // Accumulate (v, 1) into samp[lab] for every active lane: one vector atomic
@@ -1296,9 +1292,14 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
         }
         const uint32_t m = cnt + ng;   // entries of the cell's collision
         if (TAPE && valid) a.tape_ncell[cur.x + lane] = m > 1 ? m : 0u;   // the adjoint tape: entries of collided cells
-        if (m > 1) {
-            const float3 ax = srd_axis_philox(b, step, ref_index(b, cc));
-            sh.axis[lane] = make_float4(ax.x, ax.y, ax.z, 0.0f);
+        {   // rotation axis (drawn for cells of more than one entry; zero for the others,
+            // whose collision result the finish discards)
+            float4 axw = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (m > 1) {
+                const float3 ax = srd_axis_philox(b, step, ref_index(b, cc));
+                axw = make_float4(ax.x, ax.y, ax.z, 0.0f);
+            }
+            sh.axis[lane] = axw;
         }
         __syncwarp();
 
@@ -1317,8 +1318,10 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
         bool next_prefetched = false;  // the next run's first batch was asked of L2
         // 32 particles at a time, across batch boundaries
         for (uint32_t g0 = 0; g0 < total; g0 += 32) {
-            const uint32_t t = g0 + lane;
-            const bool active = t < total;
+            // lanes past the run's last particle redo that particle and write nothing
+            // (no branch around the particle's work)
+            const bool active = g0 + lane < total;
+            const uint32_t t = active ? g0 + lane : total - 1u;
             // cells of the group's first and last particles: the cells that end at or before them
             const uint32_t lo = __popc(__ballot_sync(kFull, incl <= g0));
             const uint32_t hi = __popc(__ballot_sync(kFull, incl <= min(g0 + 31u, total - 1u)));
@@ -1400,22 +1403,27 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
             const uint32_t slot = __shfl_sync(kFull, rel, (int)(i & 31u)) + t;
             uint32_t key = 0, id = 0;
             float3 xn = make_float3(0, 0, 0), vn = xn;
-            if (active) {
+            {
                 float4 xp, vp;
                 load_slot(a.in_slots + slot, xp, vp);
                 const float4 cd = sh.cell[i];
+                const float4 ax = sh.axis[i];
                 float3 x = make_float3(xp.x, xp.y, xp.z), v = make_float3(vp.x, vp.y, vp.z);
-                if (__float_as_uint(cd.w) > 1) {
-                    const float4 ax = sh.axis[i];
-                    srd_collide(b, s, make_float3(cd.x, cd.y, cd.z), make_float3(ax.x, ax.y, ax.z), x, v);
+                {   // the collision computed for every lane, kept where the cell has more than one
+                    // entry (a lone particle keeps its shifted position, as in the reference)
+                    float3 xc = x, vc = v;
+                    srd_collide(b, s, make_float3(cd.x, cd.y, cd.z), make_float3(ax.x, ax.y, ax.z), xc, vc);
+                    const bool collided = __float_as_uint(cd.w) > 1;
+                    x = collided ? xc : x;
+                    v = collided ? vc : v;
                 }
                 vn = v;
                 xn = stream_shift(b, x, vn, sn);
                 key = b.cell_base + storage_index(b, cell_of_wrapped(b, xn));
                 id = __float_as_uint(vp.w);
                 const uint32_t lab = SAMPLE || TAPE ? b.cell_base + storage_index(b, cell_of_wrapped(b, x)) : 0u;
-                if (SAMPLE) sample_add(a.samp, lab, v, true);
-                if (TAPE) {   // collision cell (or none), lab cell and the bounce of the streaming that follows
+                if (SAMPLE) sample_add(a.samp, lab, v, active);
+                if (TAPE && active) {   // collision cell (or none), lab cell and the bounce of the streaming that follows
                     const bool bounced = vn.x != v.x || vn.y != v.y || vn.z != v.z;
                     a.tape_key[id] = __float_as_uint(cd.w) > 1 ? cur.x + i : kTapeNone;
                     a.tape_lab[id] = lab | (bounced ? kTapeBounce : 0u);
