@@ -198,14 +198,12 @@ __device__ __forceinline__ void store_particle(const StepArgs& a, const BoxDesc&
                                                uint32_t key, bool active)
 {
     const uint32_t slot = claim_slot(a.out_count, key, active);
-    if (!active) return;
     const float4 xp = make_float4(xs.x, xs.y, xs.z, __uint_as_float(kNoExt));
     const float4 vp = make_float4(vs.x, vs.y, vs.z, __uint_as_float(id));
-    if (slot < b.depth) {
-        store_slot(a.out_slots + b.slot_base + (uint64_t)(key - b.cell_base) * b.depth + slot, xp, vp);
-    } else {
-        push_overflow(a, key, xp, vp);
-    }
+    // the slot's index in 32 bits: every bucket slot index is below 2^32 (the engine checks)
+    const uint32_t index = (uint32_t)b.slot_base + (key - b.cell_base) * b.depth + slot;
+    if (active && slot < b.depth) store_slot(a.out_slots + index, xp, vp);
+    if (__builtin_expect(active && slot >= b.depth, 0)) push_overflow(a, key, xp, vp);
 }
 
 // The colliding particles of box-local cell `local` (raw count `raw`): returns
