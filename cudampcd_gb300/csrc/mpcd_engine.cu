@@ -158,11 +158,15 @@ public:
                 continue;
             }
             ++i;
-            launch_one_step(sample);
+            const uint64_t k = step_;
+            // a sampled run-kernel step folds the previous step's sample itself; the
+            // first sample after a restart (snapshot) and other kernels fold their own now
+            const bool folded = launch_one_step(sample, sample && !snapshot);
             if (sample) {
-                check(launch_sample_finalize(samp_.as<float4>(), acc_.as<SampleAcc>(), cells_, snapshot ? 1 : 0,
-                                             sms_ * 8, stream_),
-                      "sample finalize");
+                if (!folded)
+                    check(launch_sample_finalize(sample_buffer(k), acc_.as<SampleAcc>(), cells_, snapshot ? 1 : 0,
+                                                 sms_ * 8, stream_),
+                          "sample finalize");
                 if (snapshot) {
                     sampling_ = true;
                     sample_counter_ = 0;
@@ -171,8 +175,16 @@ public:
                 }
             }
         }
+        // the last step's sample (its buffer is clear if that step folded it already)
+        if (sample && n > 0)
+            check(launch_sample_finalize(sample_buffer(step_ - 1), acc_.as<SampleAcc>(), cells_, 0, sms_ * 8, stream_),
+                  "sample finalize");
         check_device_errors();
     }
+
+    // The lab-grid sums of step k: two buffers by step parity, so that a sampled step
+    // can fold the previous step's while it fills its own.
+    float4* sample_buffer(uint64_t k) const { return samp_.as<float4>() + (k & 1) * cells_; }
 
     // Mean fields of the FP64 sums (kept in storage order), gathered into the
     // reference order on the device: 16 bytes per cell cross to the host.
@@ -670,7 +682,7 @@ public:
         std::vector<cudaEvent_t> ks(2 * (size_t)n);
         for (auto& e : ks) check(cudaEventCreate(&e), "event");
         check(cudaEventRecord(e0, stream_), "event");
-        for (int i = 0; i < n; ++i) launch_one_step(false, ks[2 * i], ks[2 * i + 1]);
+        for (int i = 0; i < n; ++i) launch_one_step(false, false, ks[2 * i], ks[2 * i + 1]);
         check(cudaEventRecord(e1, stream_), "event");
         check(cudaEventSynchronize(e1), "event");
         float t = 0, k = 0;
@@ -993,7 +1005,7 @@ private:
         if (boxes_.size() > 1) check(box_shifts_.alloc(sizeof(float4) * 2 * boxes_.size()), "alloc box shifts");
         check(state_.alloc(sizeof(DeviceState)), "alloc state");
         check(cudaMemset(state_.p, 0, sizeof(DeviceState)), "clear state");
-        check(samp_.alloc(sizeof(float4) * cells_), "alloc sample");
+        check(samp_.alloc(sizeof(float4) * cells_ * 2), "alloc sample");   // two parities
         check(cudaMemset(samp_.p, 0, samp_.bytes), "clear sample");
         check(acc_.alloc(sizeof(SampleAcc) * cells_), "alloc sample sums");
         check(cudaMemset(acc_.p, 0, acc_.bytes), "clear sample sums");
@@ -1085,7 +1097,9 @@ private:
         a.ov_next_in = ov_next_[p].as<uint32_t>();
         a.ov_next_out = ov_next_[q].as<uint32_t>();
         a.state = state_.as<DeviceState>();
-        a.samp = samp_.as<float4>();
+        a.samp = sample_buffer(k);
+        a.acc = acc_.as<SampleAcc>();
+        a.fold_samp = nullptr;
         std::memcpy(a.ext_axis, ext_axis_, sizeof ext_axis_);
         a.draws = tables_;
         a.replay = replay ? 1 : 0;
@@ -1132,10 +1146,11 @@ private:
             a.step_base = step_base_ptr();
             a.sample = sample ? 1 : 0;
             use_run_kernel_ghosts(a, false);
+            if (sample && a.run_kernel) a.fold_samp = sample_buffer((uint64_t)i + 1);   // the other parity: step i-1's
             err = select_overflow(a, (uint64_t)i, cs);
             if (err == cudaSuccess) err = launch_step(a, params_.algorithm, false, pbuf_, grid_, cs, &branches_);
-            if (err == cudaSuccess && sample)
-                err = launch_sample_finalize(samp_.as<float4>(), acc_.as<SampleAcc>(), cells_, 0, sms_ * 8, cs);
+            if (err == cudaSuccess && sample && !a.fold_samp)
+                err = launch_sample_finalize(a.samp, acc_.as<SampleAcc>(), cells_, 0, sms_ * 8, cs);
         }
         if (err == cudaSuccess) err = launch_advance(state_.as<DeviceState>(), kGraphSteps, cs);
         cudaGraph_t graph = nullptr;
@@ -1184,11 +1199,14 @@ private:
 
     // One step: the overflow selection, then the step kernel (bracketed by the
     // events `before` and `after` when given, which time the step kernel alone).
-    void launch_one_step(bool sample, cudaEvent_t before = nullptr, cudaEvent_t after = nullptr)
+    // fold: a sampled step may fold the previous step's sample (the other parity's
+    // buffer) into the FP64 sums itself; returns whether it did (run kernel only).
+    bool launch_one_step(bool sample, bool fold = false, cudaEvent_t before = nullptr, cudaEvent_t after = nullptr)
     {
         StepArgs a = args(step_);
         a.sample = sample ? 1 : 0;
         use_run_kernel_ghosts(a, use_table_);
+        if (sample && fold && a.run_kernel) a.fold_samp = sample_buffer(step_ + 1);
         check(select_overflow(a, step_, stream_), "overflow selection");
         if (before) check(cudaEventRecord(before, stream_), "event");
         check(launch_step(a, params_.algorithm, use_table_, pbuf_, grid_, stream_, &branches_), "step kernel");
@@ -1197,6 +1215,7 @@ private:
         use_table_ = false;
         ++step_;
         dense_valid_ = false;
+        return a.fold_samp != nullptr;
     }
 
     // The post-step state, by particle id, in dense_pos_ / dense_vel_: recompute
@@ -1250,7 +1269,7 @@ private:
             use_run_kernel_ghosts(a, false);   // the run kernel records the tape of single-box SRD steps
             check(select_overflow(a, step_, stream_), "overflow selection");
             check(launch_step(a, params_.algorithm, false, pbuf_, grid_, stream_), "tape step");
-            check(launch_sample_finalize(samp_.as<float4>(), acc_.as<SampleAcc>(), cells_, 1, sms_ * 8, stream_,
+            check(launch_sample_finalize(a.samp, acc_.as<SampleAcc>(), cells_, 1, sms_ * 8, stream_,
                                          tcnt_.as<uint32_t>() + (size_t)i * cells_),
                   "tape sample");
             ++step_;

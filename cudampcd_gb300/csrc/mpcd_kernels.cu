@@ -169,6 +169,28 @@ __device__ __forceinline__ uint32_t claim_slot(uint32_t* count, uint32_t key, bo
     return base + (uint32_t)__popc(peers & lanemask_lt());
 }
 
+// Fold one step's sample of lab cell c into the FP64 running sums: the cell's mean
+// velocity (0 for an empty cell, as averageReduceOnly) and its count, snapshot or
+// accumulate (cpu_backend.cpp:189-211), and clear the step's sums.
+__device__ __forceinline__ void fold_sample(float4* samp, SampleAcc* acc, uint64_t c, int snapshot,
+                                            uint32_t* lab_count)
+{
+    const float4 s = samp[c];
+    if (lab_count) lab_count[c] = (uint32_t)s.w;   // adjoint tape: particles sampled in the cell
+    float mx = s.x, my = s.y, mz = s.z;
+    if (s.w > 0.0f) {
+        const float inv = 1.0f / s.w;
+        mx *= inv; my *= inv; mz *= inv;
+    }
+    SampleAcc r = snapshot ? SampleAcc{0, 0, 0, 0} : acc[c];
+    r.n += (double)s.w;
+    r.vx += (double)mx;
+    r.vy += (double)my;
+    r.vz += (double)mz;
+    acc[c] = r;
+    samp[c] = make_float4(0, 0, 0, 0);
+}
+
 // Accumulate (v, 1) into samp[lab] for every active lane: one vector atomic
 // (red.global.add.v4.f32) per particle.
 __device__ __forceinline__ void sample_add(float4* samp, uint32_t lab, float3 v, bool active)
@@ -1266,6 +1288,9 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
         const uint32_t cnt = cell_source(a, b, a.in_slots, c, raw_next, src_lane);
         const uint32_t src_slot = (uint32_t)(src_lane - a.in_slots);
         if (valid) a.zero_count[cur.x + lane] = 0;   // counts of step k-1: step k+1 fills them
+        // sampled steps: the previous step's sample of this lane's (lab) cell into the
+        // FP64 sums, where the engine defers it to this step (every cell is one lane's)
+        if (SAMPLE && !TAPE && a.fold_samp && valid) fold_sample(a.fold_samp, a.acc, cur.x + lane, 0, nullptr);
         next = run_entry<SINGLE>(a, run + warps < run_end ? run + warps : a.num_runs);
         raw_next = lane < (next.y & 63u) ? a.in_count[next.x + lane] : 0u;
         const uint3 cc = storage_coords(b, valid ? c : 0u);
@@ -1601,29 +1626,13 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(StepArgs a, const flo
 
 // ------------------------------------------------------------------ sampling
 
-// Per lab cell: mean velocity of the step (0 for an empty cell, as averageReduceOnly)
-// into the FP64 running sums; snapshot or accumulate (cpu_backend.cpp:189-211).
-// Any cell order (the sums are kept in storage order).
+// Per lab cell: fold_sample.  Any cell order (the sums are kept in storage order).
 __global__ void sample_finalize_kernel(float4* samp, SampleAcc* acc, uint64_t cells, int snapshot,
                                        uint32_t* lab_count)
 {
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells;
-         c += (uint64_t)gridDim.x * blockDim.x) {
-        const float4 s = samp[c];
-        if (lab_count) lab_count[c] = (uint32_t)s.w;   // adjoint tape: particles sampled in the cell
-        float mx = s.x, my = s.y, mz = s.z;
-        if (s.w > 0.0f) {
-            const float inv = 1.0f / s.w;
-            mx *= inv; my *= inv; mz *= inv;
-        }
-        SampleAcc r = snapshot ? SampleAcc{0, 0, 0, 0} : acc[c];
-        r.n += (double)s.w;
-        r.vx += (double)mx;
-        r.vy += (double)my;
-        r.vz += (double)mz;
-        acc[c] = r;
-        samp[c] = make_float4(0, 0, 0, 0);
-    }
+         c += (uint64_t)gridDim.x * blockDim.x)
+        fold_sample(samp, acc, c, snapshot, lab_count);
 }
 
 // Mean fields of one box in reference order (x fastest) from the FP64 sums, which

@@ -170,6 +170,10 @@ struct StepArgs {
     DeviceState* state;
     int32_t sample;               // accumulate the lab-grid sample of clean(k+1)
     float4* samp;                 // [global lab cells, storage order] (sum vx, vy, vz, count)
+    // srd_run_kernel sampled steps: the previous step's sample (the other parity's
+    // buffer) to fold into acc, or null (the engine folds it with sample_finalize_kernel)
+    float4* fold_samp;
+    SampleAcc* acc;
     float ext_axis[13][3];        // discrete axis set of the extended collision
     DrawTables draws;             // used by the injected-draw instantiation
     // adjoint tape of this step, by particle id / cell (null: not recorded):
