@@ -100,7 +100,10 @@ __device__ __noinline__ float3 pbc_general(const BoxDesc& b, float3 r)
 __device__ __forceinline__ float3 pbc(const BoxDesc& b, float3 r)
 {
     const float ax = r.x + b.L15[0], ay = r.y + b.L15[1], az = r.z + b.L15[2];
-    const bool in = (ax >= 0.0f) & (ax < b.L3x[0]) & (ay >= 0.0f) & (ay < b.L3x[1]) & (az >= 0.0f) & (az < b.L3x[2]);
+    // 0 <= a < 3L as one unsigned compare of the bits per axis (non-negative floats
+    // order as their bits; negative values, -0 and NaN fail and take the general path)
+    const bool in = (__float_as_uint(ax) < __float_as_uint(b.L3x[0])) & (__float_as_uint(ay) < __float_as_uint(b.L3x[1])) &
+                    (__float_as_uint(az) < __float_as_uint(b.L3x[2]));
     if (__builtin_expect(in, 1))
         return make_float3(pbc1_fast(ax, b.Lf[0], b.L2x[0]) - b.Lh[0], pbc1_fast(ay, b.Lf[1], b.L2x[1]) - b.Lh[1],
                            pbc1_fast(az, b.Lf[2], b.L2x[2]) - b.Lh[2]);
