@@ -293,16 +293,16 @@ constexpr float kFixScale = 16777216.0f;   // 2^24
 __device__ __forceinline__ long long fixed24(float v) { return __float2ll_rn(v * kFixScale); }
 
 // The same value through the 32-bit conversion (the 64-bit one runs on the
-// narrow FP64 pipe); exact while |v| < 32, and the largest magnitude converted
-// is tracked in `mx` so that a caller can redo its sums with fixed24 when it
-// reaches 2^29 (|v| >= 32, or a saturated conversion).
-__device__ __forceinline__ int fixed24_narrow(float v, unsigned& mx)
+// narrow FP64 pipe); exact while |v| < 32.  The largest |v| converted is tracked
+// in `mx` (one max with an absolute-value operand) so that a caller can redo its
+// sums with fixed24 when it reaches 32: then round(v 2^24) >= 2^29 in magnitude,
+// or the conversion saturated (an infinity); a NaN converts to 0 and is ignored.
+__device__ __forceinline__ int fixed24_narrow(float v, float& mx)
 {
-    const int r = __float2int_rn(v * kFixScale);
-    mx = max(mx, r < 0 ? 0u - (unsigned)r : (unsigned)r);
-    return r;
+    mx = fmaxf(mx, fabsf(v));
+    return __float2int_rn(v * kFixScale);
 }
-constexpr unsigned kNarrowLimit = 1u << 29;   // four narrow values still sum in 32 bits
+constexpr float kNarrowLimit = 32.0f;   // below it, four narrow values still sum in 32 bits
 
 // Mean velocity of a cell of n > 1 entries (particles and ghosts) from its exact sums.
 __device__ __forceinline__ float3 srd_mean(long long sx, long long sy, long long sz, uint32_t n)
@@ -1366,7 +1366,7 @@ __global__ void __launch_bounds__(kThreads, 4) srd_run_kernel(const StepArgs a, 
                 const uint32_t cntL = __shfl_sync(kFull, cnt, (int)L), mL = __shfl_sync(kFull, m, (int)L);
                 const Slot* src = a.in_slots + __shfl_sync(kFull, src_slot, (int)L);
                 long long sx = 0, sy = 0, sz = 0;
-                unsigned mx = 0;
+                float mx = 0.0f;
                 for (uint32_t j = jl; j < cntL; j += 4 * kBatchLanes) {   // four loads in flight per lane
                     float4 v[4];
 #pragma unroll

@@ -265,6 +265,39 @@ def test_extreme_densities_and_thin_boxes_match_oracle(name):
     h.close()
 
 
+def test_fast_particles_take_the_64_bit_sums():
+    """Speeds of 32 and more (1 % of the particles at |vx| = 40): the run kernel's
+    SRD cell sums leave their 32-bit fast path for 64-bit sums.  Two production
+    steps; the getters replay a step with the tile kernel, so the second step (whose
+    inputs are the run kernel's output of the first) is compared with the oracle's
+    restatement of the reference step (Philox draw model) applied to the state read
+    after the first."""
+    box = O.Box(L=(8, 8, 8), periodic=(1, 1, 1), algorithm=O.SRD, n=10, dt=0.005, drag=0.0)
+    seed = 91
+    h = make(box, seed=seed)
+    try:
+        pos, vel, _ = O.distribute(box, h.N, 7, 8)
+        fast = np.arange(0, h.N, 100)
+        vel = vel.copy()
+        vel[fast, 0] = np.where(fast % 200 == 0, 40.0, -40.0).astype(np.float32)
+        set_state(h, pos, vel)
+        h.step(1)
+        pos, vel = h.positions(), h.velocities()
+        assert (np.abs(vel) >= 32.0).sum() >= len(fast) // 2   # still fast after one collision
+        k = h.step_index
+        s0 = h.shift(k)
+        h.step(1)
+        gp, gv = h.positions(), h.velocities()
+        tp, tv, tc, counter, table = O.translate(box, pos, vel, s0)
+        op, ov, _ = O.collide(box, tp, tv, tc, counter, table, s0, O.Draws.empty(box), O.DRAWS_PHILOX, seed=seed,
+                              step=k)
+        assert rel_err(gp, op, 1.0).max() <= REL_TOL
+        assert rel_err(gv, ov, box.thermal_velocity).max() <= REL_TOL
+        assert h.counters()[1] == 0
+    finally:
+        h.close()
+
+
 # Boxes large enough that every CTA of the persistent step kernel (4 per SM x 152
 # SMs) sweeps many tiles: the next-tile locator, the one-tile-ahead count prefetch,
 # the in-sweep clearing of the previous step's counts and the overflow chains all
