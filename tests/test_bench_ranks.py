@@ -68,3 +68,19 @@ def test_reference_arm_prints_on_rank_zero_only():
     with redirect_stdout(buf):
         bench.run_reference_arm(args, rank=1)
     assert buf.getvalue() == ""
+
+
+def test_device_memory_block_at_config_2():
+    """The bench line's bucket figures: depth min(4n, n + ceil(4 sqrt(n)) + 2) slots of
+    32 B per cell and parity, plus the extension area; 56.6 GB at config 2 against
+    112.6 GB at the reference's 4n."""
+    import bench
+
+    cells, n = 1000 * 1000 * 22, 20
+    m = bench.device_memory(int(68.5e9), n, cells, 1000 * 1000 * 20 * n)
+    assert m["bucket_depth"] == 40 and m["bucket_depth_reference"] == 80
+    assert abs(m["buckets_gb"] - 56.59) < 0.01
+    assert abs(m["buckets_gb_at_reference_depth"] - 112.64) < 0.01
+    for k in (1, 2, 3, 5, 10, 64, 409):
+        d = bench.device_memory(0, k, 1000, 1000 * k)["bucket_depth"]
+        assert k < d <= 4 * k or k == 1 and d == 4
